@@ -1,0 +1,168 @@
+"""CPU oracle for the force-model SGD embedding step.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
+checker and by bench.py's CPU legs.  The product (distembed_gb300) never
+imports it.
+
+Two libraries live here:
+  liboracle.so       the FP64 restatement (de_oracle.cpp), built anywhere g++ exists
+  _ref/libderef.so   the reference's own code compiled against oracle/shim/; it can
+                     only be built where the reference sources are (see Makefile)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def _p(a, t=ctypes.c_void_p):
+    return ctypes.cast(a.ctypes.data, t) if a is not None else None
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (and the reference harness when ref=True)."""
+    subprocess.check_call(["make", "-s", "-C", HERE] + (["all", "ref"] if ref else ["all"]))
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.oracle_negatives.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _i64p]
+        L.oracle_rep_rows.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_batch_grad.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, _f64p, _f64p]
+        L.oracle_run.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int]
+        _LIB = L
+    return _LIB
+
+
+def ref_path() -> str:
+    return os.path.join(HERE, "_ref", "libderef.so")
+
+
+def ref_available() -> bool:
+    return os.path.exists(ref_path())
+
+
+def ref():
+    """The reference's own code (shim-compiled); raises if it was not built here."""
+    global _REF
+    if _REF is None:
+        L = ctypes.CDLL(ref_path())
+        L.deref_run.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p,
+                                ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int]
+        L.deref_batch_grad.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, _f64p]
+        L.deref_negatives.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_uint64)]
+        L.deref_csr.argtypes = [ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _i64p, _i64p]
+        _REF = L
+    return _REF
+
+
+def _csr(rowptr, col):
+    return (np.ascontiguousarray(rowptr, dtype=np.int64), np.ascontiguousarray(col, dtype=np.int64))
+
+
+# ---------------------------------------------------------------- restatement
+
+def negatives(n: int, seed: int, ns: int) -> np.ndarray:
+    out = np.zeros(max(ns, 1), dtype=np.int64)
+    lib().oracle_negatives(n, seed, ns, _p(out, _i64p))
+    return out[:ns]
+
+
+def rep_rows(n: int, batch: int, epoch_in_call: int, batch_id: int, quirks: bool) -> int:
+    return lib().oracle_rep_rows(n, batch, epoch_in_call, batch_id, int(quirks))
+
+
+def batch_grad(rowptr, col, x, batch, ns, lr, batch_id, seed, rep, quirks=True):
+    """One minibatch's update before it is applied; returns (prev[batch, dim], row_loss[batch])."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, dim = x.shape
+    prev = np.zeros((batch, dim), dtype=np.float64)
+    rl = np.zeros(batch, dtype=np.float64)
+    rc = lib().oracle_batch_grad(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), batch, ns, lr,
+                                 batch_id, seed, rep, int(quirks), _p(prev, _f64p), _p(rl, _f64p))
+    if rc != 0:
+        raise ValueError(f"oracle_batch_grad failed ({rc})")
+    return prev, rl
+
+
+def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0):
+    """Runs `epochs` epochs; returns (x_new, loss_per_epoch).  lr: scalar or per-epoch array."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.array(x, dtype=np.float64, order="C", copy=True)
+    n, dim = x.shape
+    lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+    loss = np.zeros(max(epochs, 1), dtype=np.float64)
+    rc = lib().oracle_run(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epochs, batch, ns,
+                          _p(lrs, _f64p), int(quirks), _p(loss, _f64p), threads)
+    if rc != 0:
+        raise ValueError(f"oracle_run failed ({rc})")
+    return x, loss[:epochs]
+
+
+# ------------------------------------------------------ the reference's code
+
+def ref_negatives(lower: int, upper: int, seed: int, ns: int) -> np.ndarray:
+    out = np.zeros(max(ns, 1), dtype=np.uint64)
+    ref().deref_negatives(lower, upper, seed, ns, _p(out, ctypes.POINTER(ctypes.c_uint64)))
+    return out[:ns]
+
+
+def ref_run(rowptr, col, x, epochs, batch, ns, lr, driver_loop=False):
+    """The reference's EmbeddingAlgo (FP64, its quirks included).  Returns x_new,
+    or None when a negative draw would hit the reference's undefined path."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.array(x, dtype=np.float64, order="C", copy=True)
+    n, dim = x.shape
+    lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+    rc = ref().deref_run(dim, n, len(col), _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), epochs,
+                         batch, ns, _p(lrs, _f64p), int(driver_loop))
+    if rc == -2:
+        return None
+    if rc != 0:
+        raise ValueError(f"deref_run failed ({rc})")
+    return x
+
+
+def ref_batch_grad(rowptr, col, x, batch, ns, lr, batch_id, seed, considering):
+    rowptr, col = _csr(rowptr, col)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, dim = x.shape
+    prev = np.zeros((batch, dim), dtype=np.float64)
+    rc = ref().deref_batch_grad(dim, n, len(col), _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), batch,
+                                ns, lr, batch_id, seed, considering, _p(prev, _f64p))
+    if rc == -2:
+        return None
+    if rc != 0:
+        raise ValueError(f"deref_batch_grad failed ({rc})")
+    return prev
+
+
+def ref_csr(n, coo_row, coo_col):
+    coo_row = np.ascontiguousarray(coo_row, dtype=np.int64)
+    coo_col = np.ascontiguousarray(coo_col, dtype=np.int64)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    col = np.zeros(max(len(coo_col), 1), dtype=np.int64)
+    ref().deref_csr(n, len(coo_col), _p(coo_row, _i64p), _p(coo_col, _i64p), _p(rowptr, _i64p), _p(col, _i64p))
+    return rowptr, col[:len(coo_col)]

@@ -1,0 +1,207 @@
+/*
+ * FP64 CPU restatement of DistEmbed's one-rank force-model SGD embedding step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
+ * legs of bench.py load this library, and only as the checker or the timed CPU
+ * baseline; the product path never calls it.
+ *
+ * Parity is pinned bit-for-bit against the reference's own code (compiled by
+ * `make -C oracle ref`) through the golden vectors in tests/golden/.
+ *
+ * Follows, line for line in arithmetic order:
+ *   epoch/minibatch loop      cpp/algo/algo.hpp:74-88, 135, 164-192
+ *   negative sampler          cpp/core/common.cpp:37-53
+ *   attractive pass           cpp/algo/algo.hpp:389-417 (dispatch), 521-584 (body)
+ *   repulsive pass            cpp/algo/algo.hpp:586-649
+ *   update                    cpp/algo/algo.hpp:651-666
+ *   clip                      cpp/algo/algo.hpp:65-72, bounds +-5 from cpp/dist_embed.cpp:341
+ * with the reference's one-rank quirks switchable (quirks = 1 reproduces them):
+ *   F7  edges into vertex n-1 are skipped: the destination filter is
+ *       `dst_id < dst_end_index` with dst_end_index = gCols - 1 (algo.hpp:399-405, 538)
+ *   F8  the repulsive row count becomes last_batch_size on the last batch of the
+ *       first epoch and is never reset (algo.hpp:135, 167-169, 188-190, 594)
+ * and one defined choice where the reference is undefined:
+ *   F9  a negative draw equal to n (the sampler's upper bound is inclusive) makes
+ *       the reference index a one-element vector out of range (algo.hpp:605-617).
+ *       Such draws contribute nothing here, in both modes.
+ * The loss (absent from the reference) is the t-distribution objective whose
+ * negative gradient is the force before clipping:
+ *   attractive pair  log(1 + r)
+ *   repulsive pair   log((1 + r) / (r + 1e-6))
+ * with r the squared distance at the values the minibatch reads, summed in FP64.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double kBound = 5.0;  // MAX_BOUND, cpp/dist_embed.cpp:341
+
+inline double clip(double v) {  // EmbeddingAlgo::scale, algo.hpp:65-72
+  if (v > kBound) return kBound;
+  if (v < -kBound) return -kBound;
+  return v;
+}
+
+void negatives(int64_t n, int seed, int ns, int64_t *out) {
+  std::minstd_rand gen(seed);
+  std::uniform_int_distribution<int> dist(0, int(n));
+  for (int k = 0; k < ns; ++k) out[k] = int64_t(dist(gen));
+}
+
+struct Batch {
+  int64_t n;
+  const int64_t *rowptr, *col;
+  int dim;
+  const double *x;     // embeddings, read only during the pass
+  int batch, batch_id;
+  double lr;
+  bool quirks;
+};
+
+// Attractive pass for one source row (algo.hpp:531-582).  Returns the FP64
+// attractive loss of the row.
+inline double attract_row(const Batch &b, int64_t i, double *prev_row, double *fd) {
+  const int D = b.dim;
+  const int64_t dst_end = b.quirks ? b.n - 1 : b.n;  // F7
+  double loss = 0.0;
+  for (int64_t e = b.rowptr[i]; e < b.rowptr[i + 1]; ++e) {
+    const int64_t dst = b.col[e];
+    if (!(dst >= 0 && dst < dst_end)) continue;
+    double attrc = 0;
+    for (int d = 0; d < D; ++d) {
+      fd[d] = b.x[i * D + d] - b.x[dst * D + d];
+      attrc += fd[d] * fd[d];
+    }
+    double d1 = -2.0 / (1.0 + attrc);
+    for (int d = 0; d < D; ++d) {
+      double l = clip(fd[d] * d1);
+      prev_row[d] = prev_row[d] + (b.lr) * l;
+    }
+    loss += std::log1p(attrc);
+  }
+  return loss;
+}
+
+// Repulsive pass for one row (algo.hpp:594-647).
+inline double repulse_row(const Batch &b, int64_t row, const int64_t *negs, int ns,
+                          double *prev_row, double *fd) {
+  const int D = b.dim;
+  double loss = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const int64_t c = negs[k];
+    if (c < 0 || c >= b.n) continue;  // F9
+    double repuls = 0;
+    for (int d = 0; d < D; ++d) {
+      fd[d] = b.x[row * D + d] - b.x[c * D + d];
+      repuls += fd[d] * fd[d];
+    }
+    double d1 = 2.0 / ((repuls + 0.000001) * (1.0 + repuls));
+    for (int d = 0; d < D; ++d) {
+      fd[d] = clip(fd[d] * d1);
+      prev_row[d] += (b.lr) * fd[d];
+    }
+    loss += std::log((1.0 + repuls) / (repuls + 0.000001));
+  }
+  return loss;
+}
+
+// One minibatch: prev = attractive + repulsive (rows < rep_rows), FP64 loss
+// per row into row_loss.  Three parallel passes, as the reference runs them.
+void batch_grad(const Batch &b, const int64_t *negs, int ns, int rep_rows, double *prev,
+                double *row_loss) {
+  const int D = b.dim;
+  const int64_t src_begin = int64_t(b.batch_id) * b.batch;
+  const int64_t src_end = std::min<int64_t>(src_begin + b.batch, b.n);  // exclusive
+  const int64_t rows = src_end - src_begin;
+  std::memset(prev, 0, sizeof(double) * size_t(b.batch) * D);
+#pragma omp parallel
+  {
+    std::vector<double> fd(D);
+#pragma omp for schedule(static)
+    for (int64_t i = src_begin; i < src_end; ++i) {
+      double l = attract_row(b, i, prev + (i - src_begin) * D, fd.data());
+      if (row_loss) row_loss[i - src_begin] = l;
+    }
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < rep_rows; ++i) {
+      double l = repulse_row(b, src_begin + i, negs, ns, prev + i * D, fd.data());
+      if (row_loss && i < rows) row_loss[i] += l;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* The reference's negative sampler: ns draws of
+ * uniform_int_distribution<int>(0, n) from minstd_rand(seed). */
+void oracle_negatives(int64_t n, int seed, int ns, int64_t *out) { negatives(n, seed, ns, out); }
+
+/* Rows of minibatch j that receive the repulsive pass, in epoch i of one call. */
+int oracle_rep_rows(int64_t n, int batch, int epoch_in_call, int batch_id, int quirks) {
+  const int batches = int(n / batch) + (n % batch ? 1 : 0);
+  const int last = (n % batch) ? int(n - int64_t(batch) * (batches - 1)) : batch;
+  if (batch_id == batches - 1) return last;
+  if (quirks && epoch_in_call > 0) return last;  // F8
+  return batch;
+}
+
+/* One minibatch's accumulated update, before it is applied (batch x dim, FP64),
+ * for batch `batch_id` drawn with `seed`; row_loss (nullable) gets each row's
+ * FP64 loss.  Returns 0, or -1 on a bad argument. */
+int oracle_batch_grad(int64_t n, const int64_t *rowptr, const int64_t *col, int dim,
+                      const double *x, int batch, int ns, double lr, int batch_id, int seed,
+                      int rep_rows, int quirks, double *prev_out, double *row_loss) {
+  if (n <= 0 || dim <= 0 || batch <= 0 || ns < 0) return -1;
+  std::vector<int64_t> negs(size_t(std::max(ns, 1)));
+  negatives(n, seed, ns, negs.data());
+  Batch b{n, rowptr, col, dim, x, batch, batch_id, lr, quirks != 0};
+  batch_grad(b, negs.data(), ns, rep_rows, prev_out, row_loss);
+  return 0;
+}
+
+/* `epochs` epochs of the one-rank embedding step in place on x (n x dim, FP64),
+ * one learning rate per epoch; loss_per_epoch (nullable) gets the FP64 loss of
+ * each epoch.  threads <= 0 keeps the OpenMP default.  Returns 0 or -1. */
+int oracle_run(int64_t n, const int64_t *rowptr, const int64_t *col, int dim, double *x,
+               int epochs, int batch, int ns, const double *lr_per_epoch, int quirks,
+               double *loss_per_epoch, int threads) {
+  if (n <= 0 || dim <= 0 || batch <= 0 || ns < 0 || epochs < 0) return -1;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+  const int batches = int(n / batch) + (n % batch ? 1 : 0);
+  std::vector<double> prev(size_t(batch) * dim);
+  std::vector<double> row_loss(static_cast<size_t>(batch));
+  std::vector<int64_t> negs(size_t(std::max(ns, 1)));
+  for (int i = 0; i < epochs; ++i) {
+    double epoch_loss = 0.0;
+    for (int j = 0; j < batches; ++j) {
+      negatives(n, i + j, ns, negs.data());
+      Batch b{n, rowptr, col, dim, x, batch, j, lr_per_epoch[i], quirks != 0};
+      const int rep_rows = oracle_rep_rows(n, batch, i, j, quirks);
+      batch_grad(b, negs.data(), ns, rep_rows, prev.data(), loss_per_epoch ? row_loss.data() : nullptr);
+      const int64_t base = int64_t(j) * batch;
+      const int64_t rows = std::min<int64_t>(base + batch, n) - base;
+#pragma omp parallel for schedule(static)
+      for (int64_t r = 0; r < rows; ++r)
+        for (int d = 0; d < dim; ++d) x[(base + r) * dim + d] += prev[r * dim + d];
+      if (loss_per_epoch)
+        for (int64_t r = 0; r < rows; ++r) epoch_loss += row_loss[r];
+    }
+    if (loss_per_epoch) loss_per_epoch[i] = epoch_loss;
+  }
+  return 0;
+}
+
+}  // extern "C"
