@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark of the force-model SGD embedding step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the FP32 plain GPU path at scale): R-MAT scale 20 (1,048,576 vertices,
+edge factor 16, a=.57 b=.19 c=.19, seed 1, symmetrised, duplicates and self-loops
+removed), dim 128, minibatch 4096, 5 shared negatives per minibatch, lr 0.02,
+a 10-epoch job; embedding initialised U[-0.5, 0.5] (seed 0).  Synthetic data.
+
+A step is one epoch of that job (256 minibatches); step k runs epoch k mod 10
+with the reference's seeds.  `value` = edge-updates/s with the graph and the
+embedding resident in HBM; `e2e` = the same metric through the reference-facing
+call (host FP64 embedding in, 10 epochs, host FP64 embedding out) with the
+host<->device copies inside the timed region.  The embedding (512 MiB) is larger
+than L2, so no flush is needed between steps.
+
+--impl reference times the reference's CPU algorithm (the FP64 oracle port in
+oracle/, OpenMP over all host cores, same loop structure as cpp/algo/algo.hpp)
+on the same workload; each step is one minibatch of the epoch.
+
+For N > 1 (torchrun) every rank runs an independent replica on its own GPU
+(the path does not shard: one resident partition); value sums over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "edge-updates/s BF16 batched vs FP32 plain on 1 GB300 at ≤1% loss gap; job p50/p99"
+UNIT = "edge-updates/s"
+W = dict(scale=20, edge_factor=16, seed=1, dim=128, batch=4096, ns=5, lr=0.02, epochs=10, init_seed=0)
+WORKLOAD = "rmat20_ef16_d128_b4096_ns5_fp32_plain"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload():
+    from distembed_gb300 import graphgen as gg
+    n, rowptr, col = gg.rmat_csr(W["scale"], W["edge_factor"], seed=W["seed"])
+    x0 = gg.init_embedding(n, W["dim"], seed=W["init_seed"])
+    return n, rowptr, col, x0
+
+
+def algorithmic_bytes_per_epoch(n, nnz_eff, batches, dim, ns, s=4):
+    """Gathers with no reuse credited: per CSR entry its column id and the
+    neighbour row; per vertex its rowptr entry, its own row read and written;
+    per minibatch the negative rows."""
+    return nnz_eff * (4 + dim * s) + n * (8 + 2 * dim * s) + batches * ns * dim * s
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "plain_batch_kernel_rmat20.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_scaled:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def cpu_sample(rowptr, col, x0, seconds):
+    """The FP64 oracle (the reference's algorithm, its OpenMP structure) on host
+    cores: stride-sampled minibatches of epoch 0 until `seconds` have passed."""
+    import oracle
+    n = len(rowptr) - 1
+    batches = (n + W["batch"] - 1) // W["batch"]
+    order = [j for s in (0, 4, 2, 6, 1, 5, 3, 7) for j in range(s, batches, 8)]
+    x = np.array(x0, dtype=np.float64, copy=True)
+    threads = os.cpu_count() or 1
+    updates, done, t0 = 0, 0, time.perf_counter()
+    for j in order:
+        updates += oracle.run_batches(rowptr, col, x, 0, W["batch"], W["ns"], W["lr"], [j], quirks=True,
+                                      threads=threads)
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": updates / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} of {batches} minibatches of epoch 0 (stride-8 order), FP64, {updates} edge-updates "
+                      f"in {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    n, rowptr, col, x0 = workload()
+    batches = (n + W["batch"] - 1) // W["batch"]
+    x = np.array(x0, dtype=np.float64, copy=True)
+    threads = os.cpu_count() or 1
+
+    def step(k):
+        j = (37 * k) % batches
+        return oracle.run_batches(rowptr, col, x, 0, W["batch"], W["ns"], W["lr"], [j], quirks=True, threads=threads)
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    updates = sum(step(args.warmup + k) for k in range(args.steps))
+    dt = time.perf_counter() - t0
+    v = updates / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)),
+                                            "step": "one minibatch of epoch 0 (j = 37k mod 256)",
+                                            "parallelism": "1 process x all host cores (OpenMP)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} minibatches, FP64, {updates} edge-updates"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import distembed_gb300 as de
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    n, rowptr, col, x0 = workload()
+    dim, B, ns, lr, E = W["dim"], W["batch"], W["ns"], W["lr"], W["epochs"]
+    batches = (n + B - 1) // B
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    h = de.Handle(rowptr, col, dim, device=local, quirks=True, compute_loss=True)
+    stream = torch.cuda.ExternalStream(h.stream, device=local)
+    h.set_embeddings(x0)
+    upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
+
+    for k in range(args.warmup):
+        h.run(1, B, ns, lr, want_loss=False, first_epoch=k % E)
+    h.sync()
+    clocks = Clocks(local)
+    events = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    events[0].record(stream)
+    for k in range(args.steps):
+        h.run(1, B, ns, lr, want_loss=False, first_epoch=k % E)
+        events[k + 1].record(stream)
+    h.sync()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    step_ms = [events[k].elapsed_time(events[k + 1]) for k in range(args.steps)]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t[0])
+    units = sum(upd[k % E] for k in range(args.steps)) * world
+    value = units / total_s
+
+    # roofline of the dominant kernel (the per-minibatch kernel: all but one
+    # launch of an epoch); per launch = epoch time / launches, gaps included
+    nnz_eff = len(col) - int(np.sum(col == n - 1))
+    alg_epoch = algorithmic_bytes_per_epoch(n, nnz_eff, batches, dim, ns)
+    mean_epoch_s = statistics.mean(step_ms) / 1e3
+    achieved = alg_epoch / mean_epoch_s / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = profile_traffic()
+
+    # end to end: the reference-facing call on pinned host FP64 buffers
+    x_host = torch.empty((n, dim), dtype=torch.float64, pin_memory=True).numpy()
+    x_host[:] = x0
+    out_host = torch.empty((n, dim), dtype=torch.float64, pin_memory=True).numpy()
+    e2e_times = []
+    for k in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.set_embeddings(x_host)
+        loss = h.run(E, B, ns, lr, want_loss=True)
+        h.get_embeddings(out=out_host)
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_times.append(t1 - t0)
+    e2e_units = sum(upd) * world
+    e2e_s = statistics.mean(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t[0])
+    h2d = n * dim * 8 + E * batches * ns * 4 + E * 4 + 8
+    d2h = n * dim * 8 + E * 8
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample(rowptr, col, x0, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: R-MAT scale 20 (ef 16, a.57 b.19 c.19, seed 1), U[-0.5,0.5] init (seed 0)",
+            "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)), "dim": dim, "batch": B, "ns": ns,
+                       "lr": lr, "epochs_per_job": E, "step": "one epoch (256 minibatches, CUDA graph)",
+                       "l2": "inputs larger than L2 (512 MiB FP32 embedding); no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU", "ref_quirks": True},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "kernel": "plain_batch_kernel<128>",
+                         "algorithmic_bytes_per_epoch": alg_epoch,
+                         "note": "achieved = algorithmic bytes / epoch time over 256 launches (gaps included)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "step": "EmbeddingAlgo call: host FP64 x in, 10 epochs, host FP64 x out (pinned)",
+                    "ms_per_step": 1e3 * e2e_s, "final_loss": float(loss[-1])},
+            "gpu_launches": args.steps * (batches + 1),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,223 @@
+"""distembed_gb300 — GB300 (sm_103a) force-model SGD graph embedding.
+
+Python mirror of DistEmbed's embedding interface over the C ABI in
+include/distembed_gb300.h (libdistembed_gb300.so, built in-tree by
+distembed_gb300.build).  Nothing here computes: every call goes to the CUDA
+library, and a missing library is an error, never a fallback.
+
+    EmbeddingAlgo   the reference's algo class (cpp/algo/algo.hpp:54-74):
+                    construct on a CSR and a dense FP64 embedding, then
+                    algo_force2_vec_ns(iterations, batch_size, ns, lr)
+                    updates the embedding in place
+    Handle          the resident-graph handle (de_create / de_run / ...)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdistembed_gb300.so")
+
+DE_OK = 0
+DE_ERR_INVALID = -1
+DE_ERR_OOM = -2
+DE_ERR_CUDA = -3
+DE_ERR_STATE = -4
+DE_ERR_UNSUPPORTED = -5
+PRECISION = {"fp32": 0, "bf16": 1}
+
+# Every entry point include/distembed_gb300.h declares.
+EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings", "de_get_embeddings",
+           "de_set_embeddings_f32", "de_get_embeddings_f32", "de_run", "de_run_from", "de_sync", "de_edge_updates",
+           "de_negatives", "de_stream", "de_last_error", "de_version")
+
+
+class DEError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("ref_quirks", ctypes.c_int32), ("compute_loss", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("stream", ctypes.c_void_p), ("max_bound", ctypes.c_double),
+                ("edge_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_i32, _i64 = ctypes.c_int32, ctypes.c_int64
+
+
+def lib():
+    """The loaded CUDA library.  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m distembed_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        L.de_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.de_default_options.restype = None
+        L.de_create.argtypes = [_i64, _vp, _vp, _i64, _i32, ctypes.POINTER(Options), ctypes.POINTER(_vp)]
+        L.de_destroy.argtypes = [_vp]
+        L.de_set_embeddings.argtypes = [_vp, _vp]
+        L.de_get_embeddings.argtypes = [_vp, _vp]
+        L.de_set_embeddings_f32.argtypes = [_vp, _vp, _i32]
+        L.de_get_embeddings_f32.argtypes = [_vp, _vp, _i32]
+        L.de_run.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp]
+        L.de_run_from.argtypes = [_vp, _i32, _i32, _i32, _i32, _vp, _vp]
+        L.de_sync.argtypes = [_vp]
+        L.de_edge_updates.argtypes = [_vp, _i32, _i32, _i32, _i32]
+        L.de_edge_updates.restype = _i64
+        L.de_negatives.argtypes = [_i64, _i32, _i32, _vp]
+        L.de_negatives.restype = None
+        L.de_stream.argtypes = [_vp]
+        L.de_stream.restype = _vp
+        L.de_last_error.argtypes = [_vp]
+        L.de_last_error.restype = ctypes.c_char_p
+        L.de_version.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> int:
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def negatives(n: int, seed: int, ns: int) -> np.ndarray:
+    """The reference's sampler (cpp/core/common.cpp:37-53), computed by the library."""
+    out = np.zeros(max(ns, 1), dtype=np.int64)
+    lib().de_negatives(n, seed, ns, out.ctypes.data)
+    return out[:ns]
+
+
+class Handle:
+    """One graph resident on one GPU, with its embedding."""
+
+    def __init__(self, rowptr, col, dim: int, precision: str = "fp32", quirks: bool = True,
+                 compute_loss: bool = True, device: int = 0, stream: int | None = None,
+                 max_bound: float = 5.0, edge_cap: int = 0):
+        L = lib()
+        self._rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        self._col = np.ascontiguousarray(col, dtype=np.int64)
+        self.n = len(self._rowptr) - 1
+        self.nnz = len(self._col)
+        self.dim = dim
+        o = Options()
+        L.de_default_options(ctypes.byref(o))
+        o.precision = PRECISION[precision]
+        o.ref_quirks = int(quirks)
+        o.compute_loss = int(compute_loss)
+        o.device = device
+        o.stream = stream
+        o.max_bound = max_bound
+        o.edge_cap = edge_cap
+        h = _vp()
+        rc = L.de_create(self.n, self._rowptr.ctypes.data, self._col.ctypes.data if self.nnz else None, self.nnz,
+                         dim, ctypes.byref(o), ctypes.byref(h))
+        if rc != DE_OK:
+            raise DEError(rc, L.de_last_error(None).decode())
+        self._h = h
+
+    def _check(self, rc: int):
+        if rc != DE_OK:
+            raise DEError(rc, lib().de_last_error(self._h).decode())
+
+    @property
+    def stream(self) -> int:
+        return lib().de_stream(self._h)
+
+    def set_embeddings(self, x):
+        """x: host FP64 (n, dim) array, host FP32 array, or a CUDA FP32 tensor."""
+        if hasattr(x, "is_cuda") and x.is_cuda:
+            assert x.dtype.__str__() == "torch.float32" and x.is_contiguous()
+            self._check(lib().de_set_embeddings_f32(self._h, x.data_ptr(), 1))
+        elif hasattr(x, "dtype") and str(x.dtype) in ("float32", "torch.float32"):
+            x = x if hasattr(x, "data_ptr") else np.ascontiguousarray(x)
+            self._check(lib().de_set_embeddings_f32(self._h, _ptr(x), 0))
+        else:
+            x = x if hasattr(x, "data_ptr") else np.ascontiguousarray(x, dtype=np.float64)
+            self._check(lib().de_set_embeddings(self._h, _ptr(x)))
+
+    def get_embeddings(self, out=None, dtype=np.float64):
+        if out is None:
+            out = np.empty((self.n, self.dim), dtype=dtype)
+        if hasattr(out, "is_cuda") and out.is_cuda:
+            self._check(lib().de_get_embeddings_f32(self._h, out.data_ptr(), 1))
+        elif str(out.dtype) in ("float32", "torch.float32"):
+            self._check(lib().de_get_embeddings_f32(self._h, _ptr(out), 0))
+        else:
+            self._check(lib().de_get_embeddings(self._h, _ptr(out)))
+        return out
+
+    def run(self, epochs: int, batch_size: int, ns: int, lr, want_loss: bool = True, first_epoch: int = 0):
+        """Runs `epochs` epochs (resumed at `first_epoch` of a call); lr is a scalar or
+        one rate per epoch run.  Returns the FP64 per-epoch loss (waits for the GPU),
+        or None when want_loss is False (returns once the work is queued on the
+        handle's stream)."""
+        lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+        loss = np.zeros(max(epochs, 1), dtype=np.float64) if want_loss else None
+        self._check(lib().de_run_from(self._h, first_epoch, epochs, batch_size, ns, lrs.ctypes.data,
+                                      loss.ctypes.data if want_loss else None))
+        return loss[:epochs] if want_loss else None
+
+    def sync(self):
+        self._check(lib().de_sync(self._h))
+
+    def edge_updates(self, epochs: int, batch_size: int, ns: int, first_epoch: int = 0) -> int:
+        return int(lib().de_edge_updates(self._h, first_epoch, epochs, batch_size, ns))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().de_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class EmbeddingAlgo:
+    """The reference's EmbeddingAlgo (cpp/algo/algo.hpp:54-74) on one GPU.
+
+    `dense` is the FP64 (n, dim) embedding, DenseMat::nCoordinates; like the
+    reference, algo_force2_vec_ns updates it in place.  The CSR is the native
+    matrix's (rowStart, col_idx).  alpha, beta and sync_comm steer the
+    multi-rank exchange, which a single resident partition does not have; they
+    are accepted and ignored.  col_major selects the reference's transposed
+    attractive traversal, which is not provided (it raises).
+    """
+
+    def __init__(self, rowptr, col, dense: np.ndarray, alpha: float = 0.0, beta: float = 0.25,
+                 max_bound: float = 5.0, min_bound: float = -5.0, col_major: bool = False,
+                 sync_comm: bool = False, *, quirks: bool = True, precision: str = "fp32",
+                 device: int = 0, stream: int | None = None, compute_loss: bool = True):
+        if col_major:
+            raise DEError(DE_ERR_UNSUPPORTED, "col_major traversal is not provided")
+        if min_bound != -max_bound:
+            raise DEError(DE_ERR_INVALID, "the reference clips to [-MAX_BOUND, MAX_BOUND]")
+        if dense.dtype != np.float64 or dense.ndim != 2 or not dense.flags.c_contiguous:
+            raise DEError(DE_ERR_INVALID, "dense must be a C-contiguous FP64 (n, dim) array")
+        self.dense = dense
+        self.handle = Handle(rowptr, col, dense.shape[1], precision=precision, quirks=quirks,
+                             compute_loss=compute_loss, device=device, stream=stream, max_bound=max_bound)
+        self.last_loss = None
+
+    def algo_force2_vec_ns(self, iterations: int, batch_size: int, ns: int, lr) -> np.ndarray:
+        self.handle.set_embeddings(self.dense)
+        self.last_loss = self.handle.run(iterations, batch_size, ns, lr, want_loss=True)
+        self.handle.get_embeddings(out=self.dense)
+        return self.last_loss

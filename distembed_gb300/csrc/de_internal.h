@@ -1,0 +1,86 @@
+// Internal types shared by the host runtime and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace de {
+
+// One unit of attractive work: row `row` (index within its minibatch) over CSR
+// entries [e_begin, e_end).  Rows whose degree exceeds the edge cap are split
+// into `nparts` items; part p of such a row writes its partial sum to slot
+// first_slot + p, and the last part to finish (counted on counters[counter])
+// adds the parts in slot order, so the result does not depend on timing.
+struct WorkItem {
+  int32_t row;
+  int32_t e_begin;
+  int32_t e_end;
+  int32_t nparts;      // 1 = whole row
+  int32_t first_slot;  // split rows: first partial slot of the row
+  int32_t part;        // split rows: index of this part
+  int32_t counter;     // split rows: arrival counter index
+  int32_t pad;
+};
+static_assert(sizeof(WorkItem) == 32, "WorkItem layout");
+
+// Work list of one minibatch size over the whole graph.
+struct Schedule {
+  int batch = 0;          // minibatch size B
+  int batches = 0;        // ceil(n / B)
+  int last_batch_size = 0;
+  int edge_cap = 0;
+  std::vector<int64_t> item_off;   // [batches + 1] into the item array
+  std::vector<int32_t> n_parts;    // partial slots used by batch j
+  std::vector<int32_t> n_split;    // split rows in batch j
+  int max_parts = 0, max_split = 0;
+  std::vector<int64_t> cta_off;    // [batches + 1] loss-partial offsets (one per CTA)
+  WorkItem *d_items = nullptr;
+  int64_t n_items = 0;
+};
+
+// Kernel arguments of one minibatch of the FP32 plain path.
+struct PlainBatchArgs {
+  float *X;                 // [n, dim] embedding; rows of batch prev are written here
+  const float *S_prev;      // staged new rows of the previous batch (read)
+  float *S_cur;             // staged new rows of this batch (write)
+  const int32_t *rowptr;    // [n + 1]
+  const int32_t *col;       // [nnz]
+  const WorkItem *items;    // this batch's work items
+  int32_t n_items;
+  int32_t base, rows;       // first row and row count of this batch
+  int32_t prev_base, prev_rows;  // previous batch (prev_rows = 0: none pending)
+  int32_t batch_id, batches, last_batch_size;
+  int32_t n;
+  int32_t quirks, compute_loss;
+  float bound;
+  const int32_t *negs;      // [epochs, batches, ns]
+  int32_t ns;
+  const float *lr;          // [epochs]
+  float *P;                 // partial slots [max_parts, dim]
+  int32_t *counters;        // [max_split]
+  double *loss_partial;     // one per CTA of the epoch
+  int64_t loss_off;
+  const int32_t *epoch;     // device [2]: epoch index within this call, first epoch of the call
+};
+
+struct FlushArgs {
+  float *X;
+  const float *S_last;
+  int32_t last_base, last_rows;
+  const double *loss_partial;
+  int64_t n_partials;
+  double *loss;             // [epochs] per-epoch loss
+  int32_t *epoch;           // device [2]; [0] incremented once per epoch
+  int32_t compute_loss;
+};
+
+// Launchers (de_plain.cu).
+cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, cudaStream_t s);
+cudaError_t launch_flush(int dim, const FlushArgs &a, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
+constexpr int kPlainWarps = 8;  // warps per CTA of the plain batch kernel
+
+}  // namespace de

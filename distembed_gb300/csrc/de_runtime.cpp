@@ -1,0 +1,526 @@
+// Host runtime of the C ABI declared in include/distembed_gb300.h.
+//
+// A handle owns one resident graph (int32 CSR on the device) and its embedding.
+// de_run mirrors EmbeddingAlgo::algo_force2_vec_ns at one rank
+// (cpp/algo/algo.hpp:74-262): batches = ceil(n / B), last_batch_size, seed =
+// epoch + batch, attractive -> repulsive -> update per minibatch, minibatches
+// strictly in order.  The minibatch sequence of one epoch is captured once per
+// (B, ns) into a CUDA graph and replayed per epoch; the epoch index, learning
+// rate and negatives are read from device memory so the same graph serves
+// every epoch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/distembed_gb300.h"
+#include "de_internal.h"
+
+using namespace de;
+
+namespace {
+thread_local std::string g_create_error;
+}
+
+struct de_handle {
+  int64_t n = 0, nnz = 0;
+  int dim = 0;
+  de_options opt{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+
+  // resident graph and embedding
+  int32_t *d_rowptr = nullptr, *d_col = nullptr;
+  float *d_x = nullptr;
+  std::vector<int64_t> rowptr;  // host copy for schedule building
+  int64_t edges_into_last = 0;  // CSR entries whose column is n-1
+
+  // per-minibatch-size state
+  Schedule sched;
+  float *d_stage[2] = {nullptr, nullptr};
+  size_t stage_cap = 0;
+  float *d_parts = nullptr;
+  size_t parts_cap = 0;
+  int32_t *d_counters = nullptr;
+  size_t counters_cap = 0;
+  double *d_loss_partial = nullptr;
+  size_t loss_partial_cap = 0;
+
+  // per-call state
+  int32_t *d_epoch = nullptr;
+  double *d_loss = nullptr;
+  size_t loss_cap = 0;
+  int32_t *d_negs = nullptr;
+  size_t negs_cap = 0;
+  float *d_lr = nullptr;
+  size_t lr_cap = 0;
+  int32_t *h_negs = nullptr;  // pinned
+  size_t h_negs_cap = 0;
+  float *h_lr = nullptr;      // pinned
+  size_t h_lr_cap = 0;
+  double *h_loss = nullptr;   // pinned
+  size_t h_loss_cap = 0;
+  int32_t *h_epoch = nullptr;  // pinned [2]: epoch within call, first epoch
+  cudaEvent_t upload_done = nullptr;
+
+  // captured epoch
+  cudaGraphExec_t graph = nullptr;
+  int graph_batch = 0, graph_ns = -1;
+
+  // FP64 <-> FP32 staging for the host embedding copies
+  double *d_stage64 = nullptr;
+  size_t stage64_cap = 0;
+};
+
+namespace {
+
+int fail(de_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg; else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(de_handle *h, cudaError_t e, const char *what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? DE_ERR_OOM : DE_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define DE_CUDA(h, call)                                  \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <typename T>
+int grow(de_handle *h, T **p, size_t *cap, size_t need, bool *moved = nullptr) {
+  if (need <= *cap && *p) return DE_OK;
+  size_t want = std::max(need, size_t(1));
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  DE_CUDA(h, cudaMalloc(reinterpret_cast<void **>(p), want * sizeof(T)));
+  *cap = want;
+  if (moved) *moved = true;
+  return DE_OK;
+}
+
+template <typename T>
+int grow_pinned(de_handle *h, T **p, size_t *cap, size_t need) {
+  if (need <= *cap && *p) return DE_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  DE_CUDA(h, cudaHostAlloc(reinterpret_cast<void **>(p), std::max(need, size_t(1)) * sizeof(T),
+                           cudaHostAllocDefault));
+  *cap = std::max(need, size_t(1));
+  return DE_OK;
+}
+
+int default_edge_cap(int dim) { return dim >= 256 ? 32 : 64; }
+
+// Work items of minibatch size B: each row of each minibatch becomes one item,
+// or ceil(deg / cap) items when its degree exceeds the cap.
+void build_schedule(const de_handle *h, int B, int cap, Schedule &s, std::vector<WorkItem> &items) {
+  s.batch = B;
+  s.batches = int(h->n / B + (h->n % B ? 1 : 0));
+  s.last_batch_size = (h->n % B) ? int(h->n - int64_t(B) * (s.batches - 1)) : B;
+  s.edge_cap = cap;
+  s.item_off.assign(s.batches + 1, 0);
+  s.n_parts.assign(s.batches, 0);
+  s.n_split.assign(s.batches, 0);
+  s.cta_off.assign(s.batches + 1, 0);
+  s.max_parts = s.max_split = 0;
+  items.clear();
+  for (int j = 0; j < s.batches; ++j) {
+    const int64_t base = int64_t(j) * B;
+    const int rows = int(std::min<int64_t>(B, h->n - base));
+    int parts = 0, split = 0;
+    for (int r = 0; r < rows; ++r) {
+      const int64_t e0 = h->rowptr[base + r], e1 = h->rowptr[base + r + 1];
+      const int64_t deg = e1 - e0;
+      if (deg <= cap) {
+        items.push_back(WorkItem{r, int32_t(e0), int32_t(e1), 1, 0, 0, 0, 0});
+      } else {
+        const int np = int((deg + cap - 1) / cap);
+        for (int p = 0; p < np; ++p) {
+          const int64_t a = e0 + int64_t(p) * cap, b = std::min<int64_t>(e1, a + cap);
+          items.push_back(WorkItem{r, int32_t(a), int32_t(b), np, parts, p, split, 0});
+        }
+        parts += np;
+        split += 1;
+      }
+    }
+    s.item_off[j + 1] = int64_t(items.size());
+    s.n_parts[j] = parts;
+    s.n_split[j] = split;
+    s.max_parts = std::max(s.max_parts, parts);
+    s.max_split = std::max(s.max_split, split);
+    const int64_t n_items = s.item_off[j + 1] - s.item_off[j];
+    s.cta_off[j + 1] = s.cta_off[j] + (n_items + kPlainWarps - 1) / kPlainWarps;
+  }
+  s.n_items = int64_t(items.size());
+}
+
+void drop_graph(de_handle *h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  h->graph = nullptr;
+  h->graph_batch = 0;
+  h->graph_ns = -1;
+}
+
+int ensure_schedule(de_handle *h, int B) {
+  const int cap = h->opt.edge_cap > 0 ? h->opt.edge_cap : default_edge_cap(h->dim);
+  if (h->sched.batch == B && h->sched.edge_cap == cap && h->sched.d_items) return DE_OK;
+  drop_graph(h);
+  if (h->sched.d_items) cudaFree(h->sched.d_items);
+  h->sched = Schedule{};
+  std::vector<WorkItem> items;
+  build_schedule(h, B, cap, h->sched, items);
+  DE_CUDA(h, cudaMalloc(&h->sched.d_items, std::max<size_t>(items.size(), 1) * sizeof(WorkItem)));
+  DE_CUDA(h, cudaMemcpy(h->sched.d_items, items.data(), items.size() * sizeof(WorkItem),
+                        cudaMemcpyHostToDevice));
+  return DE_OK;
+}
+
+void draw_negatives(int64_t n, int seed, int ns, int32_t *out) {
+  std::minstd_rand gen(seed);
+  std::uniform_int_distribution<int> dist(0, int(n));
+  for (int k = 0; k < ns; ++k) out[k] = dist(gen);
+}
+
+int capture_epoch(de_handle *h, int ns) {
+  const Schedule &s = h->sched;
+  cudaStream_t st = h->stream;
+  DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int j = 0; j < s.batches && err == cudaSuccess; ++j) {
+    PlainBatchArgs a{};
+    a.X = h->d_x;
+    a.S_prev = h->d_stage[(j + 1) & 1];
+    a.S_cur = h->d_stage[j & 1];
+    a.rowptr = h->d_rowptr;
+    a.col = h->d_col;
+    a.items = s.d_items + s.item_off[j];
+    a.n_items = int32_t(s.item_off[j + 1] - s.item_off[j]);
+    a.base = int32_t(int64_t(j) * s.batch);
+    a.rows = int32_t(std::min<int64_t>(s.batch, h->n - a.base));
+    a.prev_base = j > 0 ? int32_t(int64_t(j - 1) * s.batch) : 0;
+    a.prev_rows = j > 0 ? s.batch : 0;
+    a.batch_id = j;
+    a.batches = s.batches;
+    a.last_batch_size = s.last_batch_size;
+    a.n = int32_t(h->n);
+    a.quirks = h->opt.ref_quirks;
+    a.compute_loss = h->opt.compute_loss;
+    a.bound = float(h->opt.max_bound);
+    a.negs = h->d_negs;
+    a.ns = ns;
+    a.lr = h->d_lr;
+    a.P = h->d_parts;
+    a.counters = h->d_counters;
+    a.loss_partial = h->d_loss_partial;
+    a.loss_off = s.cta_off[j];
+    a.epoch = h->d_epoch;
+    const int grid = int(s.cta_off[j + 1] - s.cta_off[j]);
+    err = launch_plain_batch(h->dim, a, grid, st);
+  }
+  if (err == cudaSuccess) {
+    FlushArgs f{};
+    f.X = h->d_x;
+    f.S_last = h->d_stage[(s.batches - 1) & 1];
+    f.last_base = int32_t(int64_t(s.batches - 1) * s.batch);
+    f.last_rows = s.last_batch_size;
+    f.loss_partial = h->d_loss_partial;
+    f.n_partials = s.cta_off[s.batches];
+    f.loss = h->d_loss;
+    f.epoch = h->d_epoch;
+    f.compute_loss = h->opt.compute_loss;
+    err = launch_flush(h->dim, f, st);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(st, &g);
+  if (err != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(h, err, "kernel launch during capture");
+  }
+  if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+  cudaError_t e3 = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e3 != cudaSuccess) {
+    h->graph = nullptr;
+    return cuda_fail(h, e3, "cudaGraphInstantiate");
+  }
+  h->graph_batch = s.batch;
+  h->graph_ns = ns;
+  return DE_OK;
+}
+
+int check_csr(de_handle *h, int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz) {
+  if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(h, DE_ERR_INVALID, "rowptr must start at 0 and end at nnz");
+  for (int64_t i = 0; i < n; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return fail(h, DE_ERR_INVALID, "rowptr must be non-decreasing");
+  for (int64_t e = 0; e < nnz; ++e)
+    if (col[e] < 0 || col[e] >= n) return fail(h, DE_ERR_INVALID, "column index out of range");
+  return DE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void de_default_options(de_options *o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = DE_PRECISION_FP32;
+  o->ref_quirks = 1;
+  o->compute_loss = 1;
+  o->device = 0;
+  o->stream = nullptr;
+  o->max_bound = 5.0;
+  o->edge_cap = 0;
+}
+
+int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
+              const de_options *opts, de_handle **out) {
+  if (!out) return fail(nullptr, DE_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (n <= 0 || nnz < 0 || !rowptr || (nnz > 0 && !col)) return fail(nullptr, DE_ERR_INVALID, "bad graph arguments");
+  if (dim != 32 && dim != 64 && dim != 128 && dim != 256)
+    return fail(nullptr, DE_ERR_INVALID, "dim must be 32, 64, 128 or 256");
+  if (n >= (int64_t(1) << 31) - 1 || nnz >= (int64_t(1) << 31) - 1)
+    return fail(nullptr, DE_ERR_UNSUPPORTED, "n and nnz must be below 2^31 - 1");
+  auto h = std::make_unique<de_handle>();
+  if (opts) h->opt = *opts; else de_default_options(&h->opt);
+  if (h->opt.precision != DE_PRECISION_FP32)
+    return fail(nullptr, DE_ERR_UNSUPPORTED, "precision not available in this build");
+  if (!(h->opt.max_bound > 0)) return fail(nullptr, DE_ERR_INVALID, "max_bound must be positive");
+  if (int rc = check_csr(h.get(), n, rowptr, col, nnz)) return fail(nullptr, rc, h->err);
+  h->n = n;
+  h->nnz = nnz;
+  h->dim = dim;
+  h->device = h->opt.device;
+  h->rowptr.assign(rowptr, rowptr + n + 1);
+  for (int64_t e = 0; e < nnz; ++e) h->edges_into_last += (col[e] == n - 1);
+
+  auto bail = [&](int rc) {
+    std::string m = h->err;
+    de_destroy(h.release());
+    return fail(nullptr, rc, m);
+  };
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return bail(cuda_fail(h.get(), e, "cudaSetDevice"));
+  if (h->opt.stream) {
+    h->stream = static_cast<cudaStream_t>(h->opt.stream);
+  } else {
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(h.get(), e, "cudaStreamCreate"));
+    h->own_stream = true;
+  }
+  std::vector<int32_t> rp32(rowptr, rowptr + n + 1), col32(col, col + nnz);
+  if ((e = cudaMalloc(&h->d_rowptr, (n + 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_col, std::max<int64_t>(nnz, 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_x, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_epoch, 2 * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaHostAlloc(&h->h_epoch, 2 * sizeof(int32_t), cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
+    return bail(cuda_fail(h.get(), e, "allocation"));
+  if ((e = cudaMemcpy(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (nnz > 0 && (e = cudaMemcpy(h->d_col, col32.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+      (e = cudaMemset(h->d_x, 0, size_t(n) * dim * sizeof(float))) != cudaSuccess)
+    return bail(cuda_fail(h.get(), e, "upload"));
+  *out = h.release();
+  return DE_OK;
+}
+
+int de_destroy(de_handle *h) {
+  if (!h) return DE_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graph(h);
+  cudaFree(h->d_rowptr);
+  cudaFree(h->d_col);
+  cudaFree(h->d_x);
+  cudaFree(h->sched.d_items);
+  cudaFree(h->d_stage[0]);
+  cudaFree(h->d_stage[1]);
+  cudaFree(h->d_parts);
+  cudaFree(h->d_counters);
+  cudaFree(h->d_loss_partial);
+  cudaFree(h->d_epoch);
+  cudaFree(h->d_loss);
+  cudaFree(h->d_negs);
+  cudaFree(h->d_lr);
+  cudaFree(h->d_stage64);
+  if (h->h_negs) cudaFreeHost(h->h_negs);
+  if (h->h_lr) cudaFreeHost(h->h_lr);
+  if (h->h_loss) cudaFreeHost(h->h_loss);
+  if (h->h_epoch) cudaFreeHost(h->h_epoch);
+  if (h->upload_done) cudaEventDestroy(h->upload_done);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return DE_OK;
+}
+
+static int copy_embeddings_f64(de_handle *h, double *host, bool to_device) {
+  if (!h || !host) return fail(h, DE_ERR_INVALID, "NULL argument");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  const int64_t total = h->n * h->dim;
+  const int64_t chunk = std::min<int64_t>(total, int64_t(8) << 20);  // 64 MiB of FP64
+  if (int rc = grow(h, &h->d_stage64, &h->stage64_cap, size_t(chunk))) return rc;
+  for (int64_t off = 0; off < total; off += chunk) {
+    const int64_t cnt = std::min(chunk, total - off);
+    if (to_device) {
+      DE_CUDA(h, cudaMemcpyAsync(h->d_stage64, host + off, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      DE_CUDA(h, launch_f64_to_f32(h->d_stage64, h->d_x + off, cnt, h->stream));
+    } else {
+      DE_CUDA(h, launch_f32_to_f64(h->d_x + off, h->d_stage64, cnt, h->stream));
+      DE_CUDA(h, cudaMemcpyAsync(host + off, h->d_stage64, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+  }
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DE_OK;
+}
+
+int de_set_embeddings(de_handle *h, const double *x) { return copy_embeddings_f64(h, const_cast<double *>(x), true); }
+int de_get_embeddings(de_handle *h, double *x) { return copy_embeddings_f64(h, x, false); }
+
+int de_set_embeddings_f32(de_handle *h, const float *x, int32_t on_device) {
+  if (!h || !x) return fail(h, DE_ERR_INVALID, "NULL argument");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  DE_CUDA(h, cudaMemcpyAsync(h->d_x, x, size_t(h->n) * h->dim * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DE_OK;
+}
+
+int de_get_embeddings_f32(de_handle *h, float *x, int32_t on_device) {
+  if (!h || !x) return fail(h, DE_ERR_INVALID, "NULL argument");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  DE_CUDA(h, cudaMemcpyAsync(x, h->d_x, size_t(h->n) * h->dim * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DE_OK;
+}
+
+int de_run(de_handle *h, int32_t epochs, int32_t batch_size, int32_t ns, const double *lr_per_epoch,
+           double *loss_per_epoch) {
+  return de_run_from(h, 0, epochs, batch_size, ns, lr_per_epoch, loss_per_epoch);
+}
+
+int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
+                const double *lr_per_epoch, double *loss_per_epoch) {
+  if (!h) return DE_ERR_INVALID;
+  if (first_epoch < 0 || epochs < 0 || batch_size <= 0 || ns < 0)
+    return fail(h, DE_ERR_INVALID, "first_epoch >= 0, epochs >= 0, batch_size > 0, ns >= 0");
+  if (epochs > 0 && !lr_per_epoch) return fail(h, DE_ERR_INVALID, "lr_per_epoch is NULL");
+  if (epochs == 0) return DE_OK;
+  DE_CUDA(h, cudaSetDevice(h->device));
+  if (int rc = ensure_schedule(h, batch_size)) return rc;
+  const Schedule &s = h->sched;
+  bool moved = false;
+  int rc = DE_OK;
+  const size_t rows_cap = size_t(s.batch) * h->dim;
+  if ((rc = grow(h, &h->d_stage[0], &h->stage_cap, rows_cap, &moved)) != DE_OK) return rc;
+  if (h->d_stage[1] == nullptr || moved) {
+    if (h->d_stage[1]) cudaFree(h->d_stage[1]);
+    h->d_stage[1] = nullptr;
+    DE_CUDA(h, cudaMalloc(&h->d_stage[1], h->stage_cap * sizeof(float)));
+    moved = true;
+  }
+  bool counters_moved = false;
+  if ((rc = grow(h, &h->d_parts, &h->parts_cap, size_t(std::max(s.max_parts, 1)) * h->dim, &moved)) ||
+      (rc = grow(h, &h->d_counters, &h->counters_cap, size_t(std::max(s.max_split, 1)), &counters_moved)) ||
+      (rc = grow(h, &h->d_loss_partial, &h->loss_partial_cap, size_t(s.cta_off[s.batches]), &moved)))
+    return rc;
+  if (counters_moved) {
+    DE_CUDA(h, cudaMemset(h->d_counters, 0, h->counters_cap * sizeof(int32_t)));
+    moved = true;
+  }
+  const size_t ecap = std::max<size_t>(size_t(epochs), 64);
+  if (size_t(epochs) > h->loss_cap || !h->d_loss)
+    if ((rc = grow(h, &h->d_loss, &h->loss_cap, ecap, &moved))) return rc;
+  if (size_t(epochs) > h->lr_cap || !h->d_lr)
+    if ((rc = grow(h, &h->d_lr, &h->lr_cap, ecap, &moved))) return rc;
+  const size_t nneg = size_t(epochs) * s.batches * std::max(ns, 1);
+  if (nneg > h->negs_cap || !h->d_negs)
+    if ((rc = grow(h, &h->d_negs, &h->negs_cap, std::max(nneg, ecap * s.batches * std::max(ns, 1)), &moved)))
+      return rc;
+  if (moved) drop_graph(h);
+
+  // Host side of the upload: wait until the previous call's copies have read
+  // the pinned buffers before overwriting them.
+  DE_CUDA(h, cudaEventSynchronize(h->upload_done));
+  if ((rc = grow_pinned(h, &h->h_negs, &h->h_negs_cap, nneg)) ||
+      (rc = grow_pinned(h, &h->h_lr, &h->h_lr_cap, size_t(epochs))) ||
+      (rc = grow_pinned(h, &h->h_loss, &h->h_loss_cap, size_t(epochs))))
+    return rc;
+  for (int i = 0; i < epochs; ++i)
+    for (int j = 0; j < s.batches; ++j)
+      draw_negatives(h->n, first_epoch + i + j, ns, h->h_negs + (size_t(i) * s.batches + j) * ns);
+  for (int i = 0; i < epochs; ++i) h->h_lr[i] = float(lr_per_epoch[i]);
+  DE_CUDA(h, cudaMemcpyAsync(h->d_negs, h->h_negs, nneg * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  DE_CUDA(h, cudaMemcpyAsync(h->d_lr, h->h_lr, epochs * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  DE_CUDA(h, cudaEventRecord(h->upload_done, h->stream));
+  h->h_epoch[0] = 0;
+  h->h_epoch[1] = first_epoch;
+  DE_CUDA(h, cudaMemcpyAsync(h->d_epoch, h->h_epoch, 2 * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+
+  if (!h->graph || h->graph_batch != s.batch || h->graph_ns != ns) {
+    drop_graph(h);
+    if ((rc = capture_epoch(h, ns))) return rc;
+  }
+  for (int i = 0; i < epochs; ++i) DE_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+  if (loss_per_epoch) {
+    DE_CUDA(h, cudaMemcpyAsync(h->h_loss, h->d_loss, epochs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    DE_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::memcpy(loss_per_epoch, h->h_loss, epochs * sizeof(double));
+  }
+  DE_CUDA(h, cudaGetLastError());
+  return DE_OK;
+}
+
+int de_sync(de_handle *h) {
+  if (!h) return DE_ERR_INVALID;
+  DE_CUDA(h, cudaSetDevice(h->device));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DE_OK;
+}
+
+int64_t de_edge_updates(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size,
+                        int32_t ns) {
+  if (!h || first_epoch < 0 || epochs < 0 || batch_size <= 0 || ns < 0) return -1;
+  const int batches = int(h->n / batch_size + (h->n % batch_size ? 1 : 0));
+  const int last = (h->n % batch_size) ? int(h->n - int64_t(batch_size) * (batches - 1)) : batch_size;
+  const int64_t attract = h->nnz - (h->opt.ref_quirks ? h->edges_into_last : 0);
+  int64_t total = attract * epochs;
+  std::vector<int32_t> negs(std::max(ns, 1));
+  for (int i = first_epoch; i < first_epoch + epochs; ++i)
+    for (int j = 0; j < batches; ++j) {
+      draw_negatives(h->n, i + j, ns, negs.data());
+      int valid = 0;
+      for (int k = 0; k < ns; ++k) valid += (negs[k] >= 0 && negs[k] < h->n);
+      const int rows = (j == batches - 1) ? last : batch_size;
+      const int rep = (h->opt.ref_quirks && i > 0) ? last : rows;
+      total += int64_t(rep) * valid;
+    }
+  return total;
+}
+
+void de_negatives(int64_t n, int32_t seed, int32_t ns, int64_t *out) {
+  std::minstd_rand gen(seed);
+  std::uniform_int_distribution<int> dist(0, int(n));
+  for (int k = 0; k < ns; ++k) out[k] = dist(gen);
+}
+
+void *de_stream(de_handle *h) { return h ? static_cast<void *>(h->stream) : nullptr; }
+
+const char *de_last_error(const de_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+const char *de_version(void) { return "distembed_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -24,8 +24,9 @@ def coo_to_csr(n: int, src: np.ndarray, dst: np.ndarray, dedup: bool = True):
     """int64 CSR (rowptr[n+1], col[nnz]) with ascending columns in each row."""
     src = np.asarray(src, dtype=np.int64)
     dst = np.asarray(dst, dtype=np.int64)
-    key = src * np.int64(n) + dst
-    key = np.unique(key) if dedup else np.sort(key, kind="stable")
+    key = np.sort(src * np.int64(n) + dst)
+    if dedup and len(key) > 1:
+        key = key[np.concatenate(([True], key[1:] != key[:-1]))]
     rows = key // n
     col = (key - rows * n).astype(np.int64)
     rowptr = np.zeros(n + 1, dtype=np.int64)

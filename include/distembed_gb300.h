@@ -1,0 +1,124 @@
+/*
+ * distembed_gb300 — C ABI of the GPU force-model SGD graph-embedding step.
+ *
+ * This library replaces the one-rank branch of DistEmbed's
+ *   template<INDEX_TYPE, VALUE_TYPE, embedding_dim> class EmbeddingAlgo
+ *     EmbeddingAlgo(SpMat* native, SpMat* receiver, SpMat* sender, DenseMat* dense,
+ *                   Process3DGrid* grid, double alpha, double beta,
+ *                   VALUE_TYPE MAX_BOUND, VALUE_TYPE MIN_BOUND, bool col_major, bool sync_comm)
+ *                                                             (cpp/algo/algo.hpp:54-63)
+ *     void algo_force2_vec_ns(int iterations, int batch_size, int ns, VALUE_TYPE lr)
+ *                                                             (cpp/algo/algo.hpp:74-262)
+ * behind plain pointers and sizes.  The graph and the embedding stay resident on
+ * one GPU between calls; nothing is partitioned and no collective runs.
+ *
+ * Data handed across (the same arrays the reference algo reads):
+ *   CSR      rowptr[n+1], col[nnz]  int64, as CSRHandle::rowStart / col_idx
+ *            (cpp/core/common.h:127-131), columns ascending within a row
+ *   x        n x dim row-major FP64, as DenseMat::nCoordinates (cpp/core/dense_mat.hpp:34)
+ *
+ * Every entry point returns DE_OK (0) or a negative DE_ERR_* code; the text of
+ * the last error of a handle is available from de_last_error().  A handle is
+ * used from one host thread at a time; all its GPU work runs on one stream.
+ */
+#ifndef DISTEMBED_GB300_H
+#define DISTEMBED_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DE_OK 0
+#define DE_ERR_INVALID (-1)     /* bad argument or unsupported shape            */
+#define DE_ERR_OOM (-2)         /* device or pinned host allocation failed      */
+#define DE_ERR_CUDA (-3)        /* CUDA runtime or kernel error                 */
+#define DE_ERR_STATE (-4)       /* call out of order (e.g. run before set)      */
+#define DE_ERR_UNSUPPORTED (-5) /* valid request this build cannot serve        */
+
+#define DE_PRECISION_FP32 0 /* FP32 embedding, FP32 arithmetic                   */
+#define DE_PRECISION_BF16 1 /* BF16 storage, FP32 master copy and accumulation  */
+
+typedef struct de_handle de_handle;
+
+typedef struct de_options {
+  int32_t precision;    /* DE_PRECISION_*                                              */
+  int32_t ref_quirks;   /* 1: reproduce the reference's one-rank behaviour exactly:    */
+                        /*    edges into vertex n-1 are skipped (algo.hpp:399-405,538) */
+                        /*    and from the second epoch of a call the repulsive pass   */
+                        /*    covers last_batch_size rows (algo.hpp:135,167-169,594)   */
+  int32_t compute_loss; /* 1: accumulate the FP64 per-epoch loss                       */
+  int32_t device;       /* CUDA device ordinal                                         */
+  void *stream;         /* cudaStream_t to run on; NULL: the handle creates its own    */
+  double max_bound;     /* clip bound of every force component (reference: 5)          */
+  int32_t edge_cap;     /* max CSR entries per work item; 0 = automatic                */
+  int32_t reserved[7];
+} de_options;
+
+/* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5. */
+void de_default_options(de_options *o);
+
+/* Uploads the CSR (n vertices, nnz entries) and prepares a handle for embeddings of
+ * width dim (32, 64, 128 or 256).  Replaces the EmbeddingAlgo constructor
+ * (cpp/algo/algo.hpp:54-63) together with the CSR build it reads
+ * (cpp/core/csr_local.hpp:37-125).  The embedding starts at zero. */
+int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
+              const de_options *opts, de_handle **out);
+
+/* Frees every device and host resource of the handle.  NULL is accepted. */
+int de_destroy(de_handle *h);
+
+/* Host FP64 n x dim row-major in/out, the layout of DenseMat::nCoordinates. */
+int de_set_embeddings(de_handle *h, const double *x);
+int de_get_embeddings(de_handle *h, double *x);
+
+/* FP32 n x dim row-major in/out; on_device = 1 when x is a device pointer. */
+int de_set_embeddings_f32(de_handle *h, const float *x, int32_t on_device);
+int de_get_embeddings_f32(de_handle *h, float *x, int32_t on_device);
+
+/* Runs `epochs` epochs of minibatch force-model SGD on the resident embedding:
+ * the body of EmbeddingAlgo::algo_force2_vec_ns (cpp/algo/algo.hpp:74-262) at one
+ * rank.  lr_per_epoch[epochs] holds one rate per epoch (the reference uses one
+ * constant rate).  Negatives are drawn exactly as the reference draws them
+ * (seed = epoch + batch, cpp/algo/algo.hpp:165-173, cpp/core/common.cpp:37-53).
+ * loss_per_epoch (nullable): when given, the call waits for the GPU and writes the
+ * FP64 loss of each epoch.  When NULL the call returns once the work is queued. */
+int de_run(de_handle *h, int32_t epochs, int32_t batch_size, int32_t ns,
+           const double *lr_per_epoch, double *loss_per_epoch);
+
+/* de_run resumed at epoch `first_epoch` of a call: epoch i of this call uses the
+ * seeds and the repulsive row count of epoch first_epoch + i, so running epochs
+ * [0, a) and then [a, b) equals one de_run of b epochs.  lr_per_epoch and
+ * loss_per_epoch are indexed from 0 (the first epoch run here).  The reference
+ * has no resume; this is the checkpoint/restart entry (state = embedding + epoch). */
+int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
+                const double *lr_per_epoch, double *loss_per_epoch);
+
+/* Waits for all queued work of the handle. */
+int de_sync(de_handle *h);
+
+/* Number of edge-updates (attractive (vertex, neighbour) plus repulsive
+ * (vertex, negative) force evaluations) that de_run_from with these arguments
+ * performs.  Negative on a bad argument. */
+int64_t de_edge_updates(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size,
+                        int32_t ns);
+
+/* The reference's negative sampler: ns draws of uniform_int_distribution<int>(0, n)
+ * from minstd_rand(seed) (cpp/core/common.cpp:37-53), on the host. */
+void de_negatives(int64_t n, int32_t seed, int32_t ns, int64_t *out);
+
+/* The cudaStream_t the handle runs on (as void*). */
+void *de_stream(de_handle *h);
+
+/* Text of the last error on h (or of the last failed de_create when h is NULL). */
+const char *de_last_error(const de_handle *h);
+
+/* Library version string. */
+const char *de_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DISTEMBED_GB300_H */

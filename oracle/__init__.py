@@ -38,7 +38,8 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(HERE, "liboracle.so")
-        if not os.path.exists(path):
+        src = os.path.join(HERE, "de_oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(src) > os.path.getmtime(path):
             build()
         L = ctypes.CDLL(path)
         L.oracle_negatives.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _i64p]
@@ -48,6 +49,10 @@ def lib():
                                         ctypes.c_int, ctypes.c_int, _f64p, _f64p]
         L.oracle_run.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
                                  ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int]
+        L.oracle_run_batches.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int]
+        L.oracle_run_batches.restype = ctypes.c_int64
         _LIB = L
     return _LIB
 
@@ -119,6 +124,19 @@ def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0):
     if rc != 0:
         raise ValueError(f"oracle_run failed ({rc})")
     return x, loss[:epochs]
+
+
+def run_batches(rowptr, col, x, epoch_in_call, batch, ns, lr, batch_ids, quirks=True, threads=0):
+    """Runs the listed minibatches of one epoch in place on x (FP64, C-contiguous);
+    returns the edge-updates performed.  Used for bounded CPU timing samples."""
+    ids = np.ascontiguousarray(batch_ids, dtype=np.int32)
+    n, dim = x.shape
+    assert x.dtype == np.float64 and x.flags.c_contiguous
+    u = lib().oracle_run_batches(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epoch_in_call, batch,
+                                 ns, lr, int(quirks), _p(ids, ctypes.POINTER(ctypes.c_int32)), len(ids), threads)
+    if u < 0:
+        raise ValueError("oracle_run_batches failed")
+    return int(u)
 
 
 # ------------------------------------------------------ the reference's code

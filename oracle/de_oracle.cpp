@@ -204,4 +204,39 @@ int oracle_run(int64_t n, const int64_t *rowptr, const int64_t *col, int dim, do
   return 0;
 }
 
+/* A bounded sample of one epoch for timing: runs only the minibatches listed in
+ * batch_ids (ascending), each exactly as oracle_run would in epoch
+ * `epoch_in_call`, updating x in place.  Returns the number of edge-updates
+ * performed (attractive entries plus repulsive (row, valid negative) pairs),
+ * or -1 on a bad argument. */
+int64_t oracle_run_batches(int64_t n, const int64_t *rowptr, const int64_t *col, int dim,
+                           double *x, int epoch_in_call, int batch, int ns, double lr, int quirks,
+                           const int32_t *batch_ids, int n_ids, int threads) {
+  if (n <= 0 || dim <= 0 || batch <= 0 || ns < 0) return -1;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+  std::vector<double> prev(size_t(batch) * dim);
+  std::vector<int64_t> negs(size_t(std::max(ns, 1)));
+  int64_t updates = 0;
+  for (int t = 0; t < n_ids; ++t) {
+    const int j = batch_ids[t];
+    negatives(n, epoch_in_call + j, ns, negs.data());
+    Batch b{n, rowptr, col, dim, x, batch, j, lr, quirks != 0};
+    const int rep_rows = oracle_rep_rows(n, batch, epoch_in_call, j, quirks);
+    batch_grad(b, negs.data(), ns, rep_rows, prev.data(), nullptr);
+    const int64_t base = int64_t(j) * batch;
+    const int64_t rows = std::min<int64_t>(base + batch, n) - base;
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < rows; ++r)
+      for (int d = 0; d < dim; ++d) x[(base + r) * dim + d] += prev[r * dim + d];
+    for (int64_t i = base; i < base + rows; ++i)
+      for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e) updates += (!quirks || col[e] < n - 1);
+    int valid = 0;
+    for (int k = 0; k < ns; ++k) valid += (negs[k] >= 0 && negs[k] < n);
+    updates += int64_t(rep_rows) * valid;
+  }
+  return updates;
+}
+
 }  // extern "C"
