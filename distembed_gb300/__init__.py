@@ -44,7 +44,7 @@ class DEError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("ref_quirks", ctypes.c_int32), ("compute_loss", ctypes.c_int32),
                 ("device", ctypes.c_int32), ("stream", ctypes.c_void_p), ("max_bound", ctypes.c_double),
-                ("edge_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("edge_cap", ctypes.c_int32), ("pdl", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 _lib = None
@@ -101,7 +101,7 @@ class Handle:
 
     def __init__(self, rowptr, col, dim: int, precision: str = "fp32", quirks: bool = True,
                  compute_loss: bool = True, device: int = 0, stream: int | None = None,
-                 max_bound: float = 5.0, edge_cap: int = 0):
+                 max_bound: float = 5.0, edge_cap: int = 0, pdl: bool = True):
         L = lib()
         self._rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
         self._col = np.ascontiguousarray(col, dtype=np.int64)
@@ -117,6 +117,7 @@ class Handle:
         o.stream = stream
         o.max_bound = max_bound
         o.edge_cap = edge_cap
+        o.pdl = int(pdl)
         h = _vp()
         rc = L.de_create(self.n, self._rowptr.ctypes.data, self._col.ctypes.data if self.nnz else None, self.nnz,
                          dim, ctypes.byref(o), ctypes.byref(h))

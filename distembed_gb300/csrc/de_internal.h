@@ -10,17 +10,23 @@ namespace de {
 
 // One unit of attractive work: row `row` (index within its minibatch) over CSR
 // entries [e_begin, e_end).  Rows whose degree exceeds the edge cap are split
-// into `nparts` items; part p of such a row writes its partial sum to slot
-// first_slot + p, and the last part to finish (counted on counters[counter])
-// adds the parts in slot order, so the result does not depend on timing.
+// into P = `nparts` items, combined in two fixed-order levels so the result does
+// not depend on timing:
+//   part p writes its partial to slot first_slot + p; parts form groups of
+//   kCombineGroup; the last part of group g to arrive (counters[counter + g])
+//   sums the group's slots in order.  With NG = ceil(P / kCombineGroup) > 1
+//   groups, that sum goes to slot first_slot + P + g and the last group to
+//   arrive (counters[counter + NG]) sums the NG group slots in order.
+// A split row uses P + (NG > 1 ? NG : 0) slots and NG + (NG > 1) counters.
+constexpr int kCombineGroup = 16;
 struct WorkItem {
   int32_t row;
   int32_t e_begin;
   int32_t e_end;
   int32_t nparts;      // 1 = whole row
-  int32_t first_slot;  // split rows: first partial slot of the row
+  int32_t first_slot;  // split rows: first slot of the row
   int32_t part;        // split rows: index of this part
-  int32_t counter;     // split rows: arrival counter index
+  int32_t counter;     // split rows: first counter of the row
   int32_t pad;
 };
 static_assert(sizeof(WorkItem) == 32, "WorkItem layout");
@@ -33,9 +39,9 @@ struct Schedule {
   int edge_cap = 0;
   std::vector<int64_t> item_off;   // [batches + 1] into the item array
   std::vector<int32_t> n_parts;    // partial slots used by batch j
-  std::vector<int32_t> n_split;    // split rows in batch j
+  std::vector<int32_t> n_split;    // arrival counters used by batch j
   int max_parts = 0, max_split = 0;
-  std::vector<int64_t> cta_off;    // [batches + 1] loss-partial offsets (one per CTA)
+  std::vector<int64_t> cta_off;    // [batches + 1] CTA counts (prefix) of the minibatch launches
   WorkItem *d_items = nullptr;
   int64_t n_items = 0;
 };
@@ -59,9 +65,9 @@ struct PlainBatchArgs {
   int32_t ns;
   const float *lr;          // [epochs]
   float *P;                 // partial slots [max_parts, dim]
-  int32_t *counters;        // [max_split]
-  double *loss_partial;     // one per CTA of the epoch
-  int64_t loss_off;
+  int32_t *counters;        // [max counters of a minibatch], zero between uses
+  double *loss_partial;     // one per work item of the epoch
+  int64_t loss_off;         // first item of this minibatch in the epoch
   const int32_t *epoch;     // device [2]: epoch index within this call, first epoch of the call
 };
 
@@ -71,16 +77,21 @@ struct FlushArgs {
   int32_t last_base, last_rows;
   const double *loss_partial;
   int64_t n_partials;
+  double *block_sums;       // [kFlushBlocks]
+  int32_t *done;            // CTA arrival counter, zero between uses
   double *loss;             // [epochs] per-epoch loss
   int32_t *epoch;           // device [2]; [0] incremented once per epoch
   int32_t compute_loss;
 };
 
-// Launchers (de_plain.cu).
-cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, cudaStream_t s);
-cudaError_t launch_flush(int dim, const FlushArgs &a, cudaStream_t s);
+constexpr int kFlushBlocks = 152;
+
+// Launchers (de_plain.cu).  pdl: launch with a programmatic dependency on the
+// previous kernel in the stream.
+cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool pdl, cudaStream_t s);
+cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
-constexpr int kPlainWarps = 8;  // warps per CTA of the plain batch kernel
+constexpr int kPlainWarps = 4;  // warps per CTA of the plain batch kernel
 
 }  // namespace de

@@ -1,19 +1,24 @@
 // FP32 plain form of the force-model SGD minibatch step (sm_103a).
 //
 // One launch per minibatch.  A warp owns one work item (a row, or an edge-capped
-// piece of a high-degree row).  Each lane holds dim/32 consecutive-ish components
-// of a row, so a neighbour row is one coalesced 128-bit load per lane at dim 128.
-// Per CSR entry the warp computes the squared distance with a shuffle reduction,
-// the t-distribution coefficient and the clipped, scaled force, and accumulates
-// it in registers (cpp/algo/algo.hpp:531-582).  The repulsive pass over the
-// minibatch's shared negatives (algo.hpp:594-647) and the update
-// (algo.hpp:651-666) are fused into the same pass.
+// piece of a high-degree row); items are sorted by decreasing cost so the block
+// scheduler hands out the long ones first.  Each lane holds dim/32 components of
+// a row, so a neighbour row is one coalesced 128-bit load per lane at dim 128.
+// Eight neighbour rows are in flight per warp; their eight squared distances are
+// reduced together (9 shuffles), each lane turns one of them into the
+// t-distribution coefficient and the coefficients are broadcast back (8
+// shuffles), then every lane clips and accumulates its components
+// (cpp/algo/algo.hpp:531-582).  The repulsive pass over the minibatch's shared
+// negatives (algo.hpp:594-647) and the update (algo.hpp:651-666) are fused into
+// the same pass.
 //
 // Within a minibatch the reference reads only pre-minibatch values (the update
 // is applied after both passes).  Here the new rows of minibatch j go to a
 // staging buffer S[j % 2]; the launch of minibatch j+1 reads rows of minibatch j
 // from that buffer and copies them back into X, so one kernel boundary per
-// minibatch is the only synchronisation.
+// minibatch is the only synchronisation.  With programmatic dependent launch the
+// next minibatch's CTAs start during this one's tail and load their static
+// inputs (work item, column ids) before waiting on it.
 #include <cuda_runtime.h>
 
 #include "de_internal.h"
@@ -97,11 +102,11 @@ __device__ __forceinline__ void store(const Frag<D> &f, float *row, int lane) {
   }
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-  return v;
-}
+// Programmatic dependent launch: allow the next kernel in the stream to start
+// scheduling, and wait for the previous one to complete with its memory visible.
+// Both are no-ops when the launch carries no programmatic dependency.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // EmbeddingAlgo::scale (cpp/algo/algo.hpp:65-72).
 __device__ __forceinline__ float clip(float v, float b) { return v > b ? b : (v < -b ? -b : v); }
@@ -113,85 +118,186 @@ __device__ __forceinline__ const float *row_ptr(const PlainBatchArgs &a, int n, 
   return off < unsigned(a.prev_rows) ? a.S_prev + size_t(off) * D : a.X + size_t(n) * D;
 }
 
+// log2 of the number of values reduced together.
+template <int U>
+struct Log2 {
+  static constexpr int value = U == 8 ? 3 : U == 4 ? 2 : U == 2 ? 1 : 0;
+  static_assert((1 << value) == U, "U must be 1, 2, 4 or 8");
+};
+
+// Sums U per-lane values over the warp at once.  Level s exchanges half of the
+// remaining values across lane bit (4 - s), so after log2(U) levels lane l holds
+// a partial of value v(l) (bits 4, 3, ... of l, most significant first); the
+// last 5 - log2(U) levels finish that sum.  Lane (u << (5 - log2 U)) ends up
+// holding the full sum of value u.
+template <int U>
+__device__ __forceinline__ float multi_warp_sum(float (&p)[U], int lane) {
+  constexpr int L = Log2<U>::value;
+#pragma unroll
+  for (int s = 0; s < L; ++s) {
+    const int m = 16 >> s;
+    const int h = U >> (s + 1);
+    const bool hi = (lane & m) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const float send = hi ? p[i] : p[i + h];
+      const float keep = hi ? p[i + h] : p[i];
+      p[i] = keep + __shfl_xor_sync(kFull, send, m);
+    }
+  }
+  float r = p[0];
+#pragma unroll
+  for (int m = 16 >> L; m >= 1; m >>= 1) r += __shfl_xor_sync(kFull, r, m);
+  return r;
+}
+
+// U pair forces between x_i and rows xn[0..U): valid_mask bit u says whether
+// pair u counts (invalid pairs must carry xn[u] == xi).  Attractive:
+// c = -2/(1+r); repulsive: c = 2/((r+1e-6)(1+r)) (algo.hpp:573, 626/641).
+// Each component is clipped and accumulated in pair order.  The loss term of a
+// pair is added on the lane that holds its full sum.
+template <int D, int U, bool kAttract>
+__device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, const Frag<D> (&xn)[U],
+                                            unsigned valid_mask, float lr, float bound, bool want_loss,
+                                            double &loss, int lane) {
+  constexpr int L = Log2<U>::value;
+  float diff[U][Frag<D>::N];
+  float p[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    p[u] = 0.f;
+#pragma unroll
+    for (int t = 0; t < Frag<D>::N; ++t) {
+      diff[u][t] = xi.v[t] - xn[u].v[t];
+      p[u] = fmaf(diff[u][t], diff[u][t], p[u]);
+    }
+  }
+  const float r = multi_warp_sum<U>(p, lane);
+  const int v = (lane >> (5 - L)) & (U - 1);
+  const bool valid = (valid_mask >> v) & 1u;
+  float c = kAttract ? -2.0f / (1.0f + r) : 2.0f / ((r + 1e-6f) * (1.0f + r));
+  if (!valid) c = 0.f;
+  if (want_loss && valid && (lane & ((32 >> L) - 1)) == 0)
+    loss += double(kAttract ? log1pf(r) : logf((1.0f + r) / (r + 1e-6f)));
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const float cu = __shfl_sync(kFull, c, u << (5 - L));
+#pragma unroll
+    for (int t = 0; t < Frag<D>::N; ++t) acc.v[t] = fmaf(lr, clip(diff[u][t] * cu, bound), acc.v[t]);
+  }
+}
+
+// acc = slot[0] + slot[1] + ... + slot[count-1], in that order; eight loads in flight.
+template <int D>
+__device__ __forceinline__ void sum_slots(Frag<D> &acc, const float *slot, int count, int lane) {
+  acc.zero();
+  for (int q0 = 0; q0 < count; q0 += 8) {
+    Frag<D> t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (q0 + u < count) load_cg(t[u], slot + size_t(q0 + u) * D, lane);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (q0 + u < count) {
+#pragma unroll
+        for (int q = 0; q < Frag<D>::N; ++q) acc.v[q] += t[u].v[q];
+      }
+  }
+}
+
+// Arrival on a split-row counter; true for the last of `expected` arrivals,
+// which also re-arms the counter.  The fences order the partial written
+// before the arrival against the reads of the last arriver.
+__device__ __forceinline__ bool arrive_last(int32_t *counter, int expected, int lane) {
+  __threadfence();
+  int old = 0;
+  if (lane == 0) old = atomicAdd(counter, 1);
+  old = __shfl_sync(kFull, old, 0);
+  if (old != expected - 1) return false;
+  __threadfence();
+  if (lane == 0) *counter = 0;
+  return true;
+}
+
+// Gathers up to U rows named by lanes [k, k+U) of `ids` (one id per lane, -1 =
+// none) and applies their forces.  Missing rows get xi (zero force).
+template <int D, int U, bool kAttract>
+__device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
+                                            int k, float lr, float bound, bool want_loss, double &loss,
+                                            int lane) {
+  Frag<D> xn[U];
+  unsigned mask = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int n = __shfl_sync(kFull, ids, k + u);
+    if (n >= 0) {
+      load_nc(xn[u], row_ptr(a, n, D), lane);
+      mask |= 1u << u;
+    } else {
+      xn[u] = xi;
+    }
+  }
+  if (mask) pair_forces<D, U, kAttract>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
+}
+
 template <int D, int U>
 __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const PlainBatchArgs a) {
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const int gw = blockIdx.x * kPlainWarps + wib;
+  const int gw = blockIdx.x * kPlainWarps + (threadIdx.x >> 5);
   const int total_w = gridDim.x * kPlainWarps;
-  const int epoch = *a.epoch;
+  const bool want_loss = a.compute_loss != 0;
+  pdl_trigger();
+
+  // ---- static inputs: readable before the previous minibatch completes
+  const bool has_item = gw < a.n_items;
+  WorkItem it{};
+  if (has_item) it = a.items[gw];
+  const int epoch = a.epoch[0];
   const float lr = a.lr[epoch];
   const float bound = a.bound;
-
-  // Rows of the previous minibatch: staging buffer -> X.  Nothing in this
-  // launch reads those rows from X.
-  for (int r = gw; r < a.prev_rows; r += total_w) {
-    Frag<D> t;
-    load_nc(t, a.S_prev + size_t(r) * D, lane);
-    store<D, false>(t, a.X + size_t(a.prev_base + r) * D, lane);
+  const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
+  const int first_cnt = has_item ? min(32, it.e_end - it.e_begin) : 0;
+  int first_cols = -1;
+  if (lane < first_cnt) {
+    first_cols = __ldg(a.col + it.e_begin + lane);
+    if (first_cols == skip) first_cols = -1;
   }
+  pdl_wait();
 
   double loss = 0.0;
-  if (gw < a.n_items) {
-    const WorkItem it = a.items[gw];
+  if (has_item) {
     const int row = a.base + it.row;
     Frag<D> xi, acc;
     load_nc(xi, a.X + size_t(row) * D, lane);
     acc.zero();
-    const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
 
     // ---- attractive pass over this item's CSR entries, in CSR order
     for (int e0 = it.e_begin; e0 < it.e_end; e0 += 32) {
       const int cnt = min(32, it.e_end - e0);
-      const int my_col = lane < cnt ? __ldg(a.col + e0 + lane) : -1;
-      for (int k = 0; k < cnt; k += U) {
-        Frag<D> xn[U];
-        int nn[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          int n = __shfl_sync(kFull, my_col, k + u);
-          if (n == skip) n = -1;
-          nn[u] = n;
-          if (n >= 0) load_nc(xn[u], row_ptr(a, n, D), lane);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (nn[u] < 0) continue;  // warp-uniform
-          float diff[Frag<D>::N];
-          float part = 0.f;
-#pragma unroll
-          for (int t = 0; t < Frag<D>::N; ++t) {
-            diff[t] = xi.v[t] - xn[u].v[t];
-            part = fmaf(diff[t], diff[t], part);
-          }
-          const float r = warp_sum(part);
-          const float c = -2.0f / (1.0f + r);
-#pragma unroll
-          for (int t = 0; t < Frag<D>::N; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, bound), acc.v[t]);
-          if (a.compute_loss && lane == 0) loss += double(log1pf(r));
-        }
+      int ids = first_cols;
+      if (e0 != it.e_begin) {
+        ids = lane < cnt ? __ldg(a.col + e0 + lane) : -1;
+        if (ids == skip) ids = -1;
       }
+      for (int k = 0; k < cnt; k += U) force_group<D, U, true>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
     }
 
-    // ---- split rows: the last part to arrive sums all parts in slot order
+    // ---- split rows: two-level, fixed-order combine of the parts
     bool owner = true;
     if (it.nparts > 1) {
+      const int P = it.nparts;
+      const int g = it.part / kCombineGroup;
+      const int ng = (P + kCombineGroup - 1) / kCombineGroup;
+      const int gsize = min(kCombineGroup, P - g * kCombineGroup);
       store<D, true>(acc, a.P + size_t(it.first_slot + it.part) * D, lane);
-      __threadfence();
-      int old = 0;
-      if (lane == 0) old = atomicAdd(a.counters + it.counter, 1);
-      old = __shfl_sync(kFull, old, 0);
-      owner = (old == it.nparts - 1);
+      owner = arrive_last(a.counters + it.counter + g, gsize, lane);
       if (owner) {
-        __threadfence();
-        acc.zero();
-        for (int p = 0; p < it.nparts; ++p) {
-          Frag<D> t;
-          load_cg(t, a.P + size_t(it.first_slot + p) * D, lane);
-#pragma unroll
-          for (int q = 0; q < Frag<D>::N; ++q) acc.v[q] += t.v[q];
+        sum_slots(acc, a.P + size_t(it.first_slot + g * kCombineGroup) * D, gsize, lane);
+        if (ng > 1) {
+          store<D, true>(acc, a.P + size_t(it.first_slot + P + g) * D, lane);
+          owner = arrive_last(a.counters + it.counter + ng, ng, lane);
+          if (owner) sum_slots(acc, a.P + size_t(it.first_slot + P) * D, ng, lane);
         }
-        if (lane == 0) a.counters[it.counter] = 0;  // ready for the next minibatch
       }
     }
 
@@ -200,23 +306,12 @@ __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const Pla
       const int rep_rows = (a.quirks && epoch + a.epoch[1] > 0) ? a.last_batch_size : a.rows;
       if (it.row < rep_rows) {
         const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
-        for (int k = 0; k < a.ns; ++k) {
-          const int n = __ldg(negs + k);
-          if (n < 0 || n >= a.n) continue;  // a draw equal to n contributes nothing
-          Frag<D> xn;
-          load_nc(xn, row_ptr(a, n, D), lane);
-          float diff[Frag<D>::N];
-          float part = 0.f;
-#pragma unroll
-          for (int t = 0; t < Frag<D>::N; ++t) {
-            diff[t] = xi.v[t] - xn.v[t];
-            part = fmaf(diff[t], diff[t], part);
-          }
-          const float r = warp_sum(part);
-          const float c = 2.0f / ((r + 1e-6f) * (1.0f + r));
-#pragma unroll
-          for (int t = 0; t < Frag<D>::N; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, bound), acc.v[t]);
-          if (a.compute_loss && lane == 0) loss += double(logf((1.0f + r) / (r + 1e-6f)));
+        for (int k0 = 0; k0 < a.ns; k0 += 32) {
+          const int cnt = min(32, a.ns - k0);
+          int ids = lane < cnt ? __ldg(negs + k0 + lane) : -1;
+          if (ids >= a.n) ids = -1;  // a draw equal to n contributes nothing
+          for (int k = 0; k < cnt; k += U)
+            force_group<D, U, false>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
         }
       }
       // ---- update, staged (algo.hpp:651-666)
@@ -227,35 +322,43 @@ __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const Pla
     }
   }
 
-  if (a.compute_loss) {
-    __shared__ double part_loss[kPlainWarps];
-    if (lane == 0) part_loss[wib] = loss;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int w = 0; w < kPlainWarps; ++w) s += part_loss[w];
-      a.loss_partial[a.loss_off + blockIdx.x] = s;
-    }
+  // Rows of the previous minibatch: staging buffer -> X.  Nothing in this
+  // launch reads those rows from X.
+  for (int r = gw; r < a.prev_rows; r += total_w) {
+    Frag<D> t;
+    load_nc(t, a.S_prev + size_t(r) * D, lane);
+    store<D, false>(t, a.X + size_t(a.prev_base + r) * D, lane);
+  }
+
+  if (want_loss && has_item) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kFull, loss, m);
+    if (lane == 0) a.loss_partial[a.loss_off + gw] = loss;
   }
 }
 
-// End of an epoch: write back the last minibatch, reduce the epoch's loss in a
-// fixed order, advance the epoch counter.
+// End of an epoch: write back the last minibatch, reduce the epoch's loss
+// partials in a fixed order (each CTA a fixed chunk, then the last CTA to
+// finish sums the chunk sums in order), advance the epoch counter.
 template <int D>
 __global__ void __launch_bounds__(256) flush_kernel(const FlushArgs a) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int total_w = gridDim.x * 8;
+  pdl_wait();
   for (int r = gw; r < a.last_rows; r += total_w) {
     Frag<D> t;
     load_nc(t, a.S_last + size_t(r) * D, lane);
     store<D, false>(t, a.X + size_t(a.last_base + r) * D, lane);
   }
-  if (blockIdx.x != 0) return;
   __shared__ double red[256];
+  __shared__ bool last;
   double s = 0.0;
-  if (a.compute_loss)
-    for (int64_t i = threadIdx.x; i < a.n_partials; i += 256) s += a.loss_partial[i];
+  if (a.compute_loss) {
+    const int64_t chunk = (a.n_partials + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = blockIdx.x * chunk, hi = min(a.n_partials, lo + chunk);
+    for (int64_t i = lo + threadIdx.x; i < hi; i += 256) s += a.loss_partial[i];
+  }
   red[threadIdx.x] = s;
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
@@ -263,9 +366,26 @@ __global__ void __launch_bounds__(256) flush_kernel(const FlushArgs a) {
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const int e = *a.epoch;
+    a.block_sums[blockIdx.x] = red[0];
+    __threadfence();
+    last = atomicAdd(a.done, 1) == int(gridDim.x) - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  s = 0.0;
+  for (int b = threadIdx.x; b < int(gridDim.x); b += 256) s += __ldcg(a.block_sums + b);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int e = a.epoch[0];
     if (a.compute_loss) a.loss[e] = red[0];
-    *a.epoch = e + 1;
+    a.epoch[0] = e + 1;
+    *a.done = 0;
   }
 }
 
@@ -279,30 +399,42 @@ __global__ void f32_to_f64_kernel(const float *__restrict__ s, double *__restric
     d[i] = double(s[i]);
 }
 
-}  // namespace
-
-cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, cudaStream_t s) {
-  const dim3 block(kPlainWarps * 32);
-  switch (dim) {
-    case 32: plain_batch_kernel<32, 8><<<grid, block, 0, s>>>(a); break;
-    case 64: plain_batch_kernel<64, 8><<<grid, block, 0, s>>>(a); break;
-    case 128: plain_batch_kernel<128, 8><<<grid, block, 0, s>>>(a); break;
-    case 256: plain_batch_kernel<256, 4><<<grid, block, 0, s>>>(a); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+template <typename Args>
+cudaError_t launch(void (*k)(Args), int grid, int block, const Args &a, bool pdl, cudaStream_t s) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, a);
 }
 
-cudaError_t launch_flush(int dim, const FlushArgs &a, cudaStream_t s) {
-  const int grid = 152;
+}  // namespace
+
+cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool pdl, cudaStream_t s) {
+  const int block = kPlainWarps * 32;
   switch (dim) {
-    case 32: flush_kernel<32><<<grid, 256, 0, s>>>(a); break;
-    case 64: flush_kernel<64><<<grid, 256, 0, s>>>(a); break;
-    case 128: flush_kernel<128><<<grid, 256, 0, s>>>(a); break;
-    case 256: flush_kernel<256><<<grid, 256, 0, s>>>(a); break;
+    case 32: return launch(plain_batch_kernel<32, 8>, grid, block, a, pdl, s);
+    case 64: return launch(plain_batch_kernel<64, 8>, grid, block, a, pdl, s);
+    case 128: return launch(plain_batch_kernel<128, 8>, grid, block, a, pdl, s);
+    case 256: return launch(plain_batch_kernel<256, 4>, grid, block, a, pdl, s);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
+}
+
+cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s) {
+  switch (dim) {
+    case 32: return launch(flush_kernel<32>, kFlushBlocks, 256, a, pdl, s);
+    case 64: return launch(flush_kernel<64>, kFlushBlocks, 256, a, pdl, s);
+    case 128: return launch(flush_kernel<128>, kFlushBlocks, 256, a, pdl, s);
+    case 256: return launch(flush_kernel<256>, kFlushBlocks, 256, a, pdl, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s) {

@@ -52,6 +52,8 @@ struct de_handle {
   size_t counters_cap = 0;
   double *d_loss_partial = nullptr;
   size_t loss_partial_cap = 0;
+  double *d_block_sums = nullptr;  // [kFlushBlocks]
+  int32_t *d_done = nullptr;       // flush arrival counter
 
   // per-call state
   int32_t *d_epoch = nullptr;
@@ -148,14 +150,19 @@ void build_schedule(const de_handle *h, int B, int cap, Schedule &s, std::vector
         items.push_back(WorkItem{r, int32_t(e0), int32_t(e1), 1, 0, 0, 0, 0});
       } else {
         const int np = int((deg + cap - 1) / cap);
+        const int ng = (np + kCombineGroup - 1) / kCombineGroup;
         for (int p = 0; p < np; ++p) {
           const int64_t a = e0 + int64_t(p) * cap, b = std::min<int64_t>(e1, a + cap);
           items.push_back(WorkItem{r, int32_t(a), int32_t(b), np, parts, p, split, 0});
         }
-        parts += np;
-        split += 1;
+        parts += np + (ng > 1 ? ng : 0);
+        split += ng + (ng > 1 ? 1 : 0);
       }
     }
+    // longest items first: the block scheduler then starts them first
+    std::stable_sort(items.begin() + s.item_off[j], items.end(), [](const WorkItem &x, const WorkItem &y) {
+      return (x.e_end - x.e_begin) > (y.e_end - y.e_begin);
+    });
     s.item_off[j + 1] = int64_t(items.size());
     s.n_parts[j] = parts;
     s.n_split[j] = split;
@@ -225,10 +232,10 @@ int capture_epoch(de_handle *h, int ns) {
     a.P = h->d_parts;
     a.counters = h->d_counters;
     a.loss_partial = h->d_loss_partial;
-    a.loss_off = s.cta_off[j];
+    a.loss_off = s.item_off[j];
     a.epoch = h->d_epoch;
     const int grid = int(s.cta_off[j + 1] - s.cta_off[j]);
-    err = launch_plain_batch(h->dim, a, grid, st);
+    err = launch_plain_batch(h->dim, a, grid, h->opt.pdl && j > 0, st);
   }
   if (err == cudaSuccess) {
     FlushArgs f{};
@@ -237,11 +244,13 @@ int capture_epoch(de_handle *h, int ns) {
     f.last_base = int32_t(int64_t(s.batches - 1) * s.batch);
     f.last_rows = s.last_batch_size;
     f.loss_partial = h->d_loss_partial;
-    f.n_partials = s.cta_off[s.batches];
+    f.n_partials = s.n_items;
+    f.block_sums = h->d_block_sums;
+    f.done = h->d_done;
     f.loss = h->d_loss;
     f.epoch = h->d_epoch;
     f.compute_loss = h->opt.compute_loss;
-    err = launch_flush(h->dim, f, st);
+    err = launch_flush(h->dim, f, h->opt.pdl != 0, st);
   }
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(st, &g);
@@ -283,6 +292,7 @@ void de_default_options(de_options *o) {
   o->stream = nullptr;
   o->max_bound = 5.0;
   o->edge_cap = 0;
+  o->pdl = 1;
 }
 
 int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
@@ -326,12 +336,15 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
       (e = cudaMalloc(&h->d_col, std::max<int64_t>(nnz, 1) * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_x, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_epoch, 2 * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_block_sums, kFlushBlocks * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_done, sizeof(int32_t))) != cudaSuccess ||
       (e = cudaHostAlloc(&h->h_epoch, 2 * sizeof(int32_t), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "allocation"));
   if ((e = cudaMemcpy(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (nnz > 0 && (e = cudaMemcpy(h->d_col, col32.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess) ||
-      (e = cudaMemset(h->d_x, 0, size_t(n) * dim * sizeof(float))) != cudaSuccess)
+      (e = cudaMemset(h->d_x, 0, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
+      (e = cudaMemset(h->d_done, 0, sizeof(int32_t))) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "upload"));
   *out = h.release();
   return DE_OK;
@@ -351,6 +364,8 @@ int de_destroy(de_handle *h) {
   cudaFree(h->d_parts);
   cudaFree(h->d_counters);
   cudaFree(h->d_loss_partial);
+  cudaFree(h->d_block_sums);
+  cudaFree(h->d_done);
   cudaFree(h->d_epoch);
   cudaFree(h->d_loss);
   cudaFree(h->d_negs);
@@ -435,7 +450,7 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
   bool counters_moved = false;
   if ((rc = grow(h, &h->d_parts, &h->parts_cap, size_t(std::max(s.max_parts, 1)) * h->dim, &moved)) ||
       (rc = grow(h, &h->d_counters, &h->counters_cap, size_t(std::max(s.max_split, 1)), &counters_moved)) ||
-      (rc = grow(h, &h->d_loss_partial, &h->loss_partial_cap, size_t(s.cta_off[s.batches]), &moved)))
+      (rc = grow(h, &h->d_loss_partial, &h->loss_partial_cap, size_t(s.n_items), &moved)))
     return rc;
   if (counters_moved) {
     DE_CUDA(h, cudaMemset(h->d_counters, 0, h->counters_cap * sizeof(int32_t)));

@@ -53,10 +53,13 @@ typedef struct de_options {
   void *stream;         /* cudaStream_t to run on; NULL: the handle creates its own    */
   double max_bound;     /* clip bound of every force component (reference: 5)          */
   int32_t edge_cap;     /* max CSR entries per work item; 0 = automatic                */
-  int32_t reserved[7];
+  int32_t pdl;          /* 1: overlap consecutive minibatch launches (programmatic     */
+                        /*    dependent launch); 0: plain stream order                 */
+  int32_t reserved[6];
 } de_options;
 
-/* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5. */
+/* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5,
+ * automatic edge cap, programmatic dependent launch on. */
 void de_default_options(de_options *o);
 
 /* Uploads the CSR (n vertices, nnz entries) and prepares a handle for embeddings of
