@@ -49,14 +49,16 @@ struct Schedule {
 // Kernel arguments of one minibatch of the FP32 plain path.
 struct PlainBatchArgs {
   float *X;                 // [n, dim] embedding; rows of batch prev are written here
-  const float *S_prev;      // staged new rows of the previous batch (read)
-  float *S_cur;             // staged new rows of this batch (write)
+  const float *S_prev2;     // staged new rows of minibatch j-2 (read)
+  const float *S_prev;      // staged new rows of minibatch j-1 (read)
+  float *S_cur;             // staged new rows of this minibatch (write)
   const int32_t *rowptr;    // [n + 1]
   const int32_t *col;       // [nnz]
   const WorkItem *items;    // this batch's work items
   int32_t n_items;
   int32_t base, rows;       // first row and row count of this batch
-  int32_t prev_base, prev_rows;  // previous batch (prev_rows = 0: none pending)
+  int32_t prev_base, prev_rows;    // minibatch j-1 (prev_rows = 0: none)
+  int32_t prev2_base, prev2_rows;  // minibatch j-2 (prev2_rows = 0: none)
   int32_t batch_id, batches, last_batch_size;
   int32_t n;
   int32_t quirks, compute_loss;
@@ -92,6 +94,8 @@ cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool 
 cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
-constexpr int kPlainWarps = 4;  // warps per CTA of the plain batch kernel
+constexpr int kPlainWarps = 4;      // warps per CTA of the plain batch kernel
+constexpr int kPlainMinBlocks = 6;  // resident CTAs per SM the register budget targets
+constexpr int kMaxEdgeCap = 32;     // CSR entries per work item: one per lane
 
 }  // namespace de

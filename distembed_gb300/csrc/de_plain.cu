@@ -13,12 +13,16 @@
 // the same pass.
 //
 // Within a minibatch the reference reads only pre-minibatch values (the update
-// is applied after both passes).  Here the new rows of minibatch j go to a
-// staging buffer S[j % 2]; the launch of minibatch j+1 reads rows of minibatch j
-// from that buffer and copies them back into X, so one kernel boundary per
-// minibatch is the only synchronisation.  With programmatic dependent launch the
-// next minibatch's CTAs start during this one's tail and load their static
-// inputs (work item, column ids) before waiting on it.
+// is applied after both passes), and minibatch j+1 must see minibatch j's update
+// (algo.hpp:164-192).  Here the new rows of minibatch j go to a staging buffer
+// S[j % 3]; launch j+1 copies them back into X, and until that copy is known to
+// be complete (two launches later) readers take those rows from S.  Launch j
+// runs in two phases around griddepcontrol.wait (programmatic dependent launch):
+// before the wait it does every force whose other row is not in minibatch j-1
+// (those rows are final), overlapping launch j-1; after the wait it does the
+// few forces into minibatch j-1, combines split rows and stores.  Launch j
+// releases launch j+1 right after its own wait, so at most two minibatches are
+// in flight and launch j+1's early phase only ever reads rows that are final.
 #include <cuda_runtime.h>
 
 #include "de_internal.h"
@@ -111,11 +115,19 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 // EmbeddingAlgo::scale (cpp/algo/algo.hpp:65-72).
 __device__ __forceinline__ float clip(float v, float b) { return v > b ? b : (v < -b ? -b : v); }
 
-// Row n as the minibatch sees it: rows of the previous minibatch still sit in
-// the staging buffer; every other row is current in X.
+__device__ __forceinline__ bool in_prev(const PlainBatchArgs &a, int n) {
+  return unsigned(n - a.prev_base) < unsigned(a.prev_rows);
+}
+
+// Row n before the wait (n is not in minibatch j-1): minibatch j-2's rows are
+// read from their staging buffer (their copy-back may be in flight), every
+// other row is final in X.  After the wait only rows of minibatch j-1 are read,
+// from their staging buffer.
+template <bool kAfterWait>
 __device__ __forceinline__ const float *row_ptr(const PlainBatchArgs &a, int n, int D) {
-  const unsigned off = unsigned(n - a.prev_base);
-  return off < unsigned(a.prev_rows) ? a.S_prev + size_t(off) * D : a.X + size_t(n) * D;
+  if (kAfterWait) return a.S_prev + size_t(n - a.prev_base) * D;
+  const unsigned off = unsigned(n - a.prev2_base);
+  return off < unsigned(a.prev2_rows) ? a.S_prev2 + size_t(off) * D : a.X + size_t(n) * D;
 }
 
 // log2 of the number of values reduced together.
@@ -221,7 +233,7 @@ __device__ __forceinline__ bool arrive_last(int32_t *counter, int expected, int 
 
 // Gathers up to U rows named by lanes [k, k+U) of `ids` (one id per lane, -1 =
 // none) and applies their forces.  Missing rows get xi (zero force).
-template <int D, int U, bool kAttract>
+template <int D, int U, bool kAttract, bool kAfterWait>
 __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
                                             int k, float lr, float bound, bool want_loss, double &loss,
                                             int lane) {
@@ -231,7 +243,8 @@ __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &ac
   for (int u = 0; u < U; ++u) {
     const int n = __shfl_sync(kFull, ids, k + u);
     if (n >= 0) {
-      load_nc(xn[u], row_ptr(a, n, D), lane);
+      if (kAfterWait) load_cg(xn[u], row_ptr<true>(a, n, D), lane);
+      else load_nc(xn[u], row_ptr<false>(a, n, D), lane);
       mask |= 1u << u;
     } else {
       xn[u] = xi;
@@ -240,15 +253,23 @@ __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &ac
   if (mask) pair_forces<D, U, kAttract>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
 }
 
+// Forces of the ids held by the warp's lanes (-1 = none), U at a time.
+template <int D, int U, bool kAttract, bool kAfterWait>
+__device__ __forceinline__ void force_lanes(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
+                                            int cnt, float lr, float bound, bool want_loss, double &loss,
+                                            int lane) {
+  for (int k = 0; k < cnt; k += U)
+    force_group<D, U, kAttract, kAfterWait>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
+}
+
 template <int D, int U>
-__global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const PlainBatchArgs a) {
+__global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBlocks)
+    plain_batch_kernel(const PlainBatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * kPlainWarps + (threadIdx.x >> 5);
   const int total_w = gridDim.x * kPlainWarps;
   const bool want_loss = a.compute_loss != 0;
-  pdl_trigger();
 
-  // ---- static inputs: readable before the previous minibatch completes
   const bool has_item = gw < a.n_items;
   WorkItem it{};
   if (has_item) it = a.items[gw];
@@ -256,31 +277,50 @@ __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const Pla
   const float lr = a.lr[epoch];
   const float bound = a.bound;
   const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
-  const int first_cnt = has_item ? min(32, it.e_end - it.e_begin) : 0;
-  int first_cols = -1;
-  if (lane < first_cnt) {
-    first_cols = __ldg(a.col + it.e_begin + lane);
-    if (first_cols == skip) first_cols = -1;
+  // this item's CSR entries, one per lane (at most 32)
+  const int cnt = has_item ? it.e_end - it.e_begin : 0;
+  int ids = -1;
+  if (lane < cnt) {
+    ids = __ldg(a.col + it.e_begin + lane);
+    if (ids == skip) ids = -1;
   }
-  pdl_wait();
+  const bool defer = ids >= 0 && in_prev(a, ids);
+  // the repulsive pass of a row is done by its part 0
+  const int rep_rows = (a.quirks && epoch + a.epoch[1] > 0) ? a.last_batch_size : a.rows;
+  const bool repulse = has_item && it.part == 0 && it.row < rep_rows;
+  const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
 
   double loss = 0.0;
+  Frag<D> xi, acc;
+  acc.zero();
   if (has_item) {
-    const int row = a.base + it.row;
-    Frag<D> xi, acc;
-    load_nc(xi, a.X + size_t(row) * D, lane);
-    acc.zero();
-
-    // ---- attractive pass over this item's CSR entries, in CSR order
-    for (int e0 = it.e_begin; e0 < it.e_end; e0 += 32) {
-      const int cnt = min(32, it.e_end - e0);
-      int ids = first_cols;
-      if (e0 != it.e_begin) {
-        ids = lane < cnt ? __ldg(a.col + e0 + lane) : -1;
-        if (ids == skip) ids = -1;
+    load_nc(xi, a.X + size_t(a.base + it.row) * D, lane);
+    // ---- before the wait: forces whose other row is final (CSR order, then draw order)
+    force_lanes<D, U, true, false>(a, acc, xi, defer ? -1 : ids, cnt, lr, bound, want_loss, loss, lane);
+    if (repulse)
+      for (int k0 = 0; k0 < a.ns; k0 += 32) {
+        const int kc = min(32, a.ns - k0);
+        int nid = lane < kc ? __ldg(negs + k0 + lane) : -1;
+        if (nid >= a.n || (nid >= 0 && in_prev(a, nid))) nid = -1;  // a draw equal to n contributes nothing
+        force_lanes<D, U, false, false>(a, acc, xi, nid, kc, lr, bound, want_loss, loss, lane);
       }
-      for (int k = 0; k < cnt; k += U) force_group<D, U, true>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
-    }
+  }
+
+  pdl_wait();
+  pdl_trigger();
+
+  if (has_item) {
+    // ---- after the wait: forces into minibatch j-1
+    if (__any_sync(kFull, defer))
+      force_lanes<D, U, true, true>(a, acc, xi, defer ? ids : -1, cnt, lr, bound, want_loss, loss, lane);
+    if (repulse && a.prev_rows > 0)
+      for (int k0 = 0; k0 < a.ns; k0 += 32) {
+        const int kc = min(32, a.ns - k0);
+        int nid = lane < kc ? __ldg(negs + k0 + lane) : -1;
+        if (!(nid >= 0 && nid < a.n && in_prev(a, nid))) nid = -1;
+        if (__any_sync(kFull, nid >= 0))
+          force_lanes<D, U, false, true>(a, acc, xi, nid, kc, lr, bound, want_loss, loss, lane);
+      }
 
     // ---- split rows: two-level, fixed-order combine of the parts
     bool owner = true;
@@ -300,21 +340,8 @@ __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const Pla
         }
       }
     }
-
+    // ---- update, staged (algo.hpp:651-666)
     if (owner) {
-      // ---- repulsive pass over the minibatch's shared negatives, in draw order
-      const int rep_rows = (a.quirks && epoch + a.epoch[1] > 0) ? a.last_batch_size : a.rows;
-      if (it.row < rep_rows) {
-        const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
-        for (int k0 = 0; k0 < a.ns; k0 += 32) {
-          const int cnt = min(32, a.ns - k0);
-          int ids = lane < cnt ? __ldg(negs + k0 + lane) : -1;
-          if (ids >= a.n) ids = -1;  // a draw equal to n contributes nothing
-          for (int k = 0; k < cnt; k += U)
-            force_group<D, U, false>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
-        }
-      }
-      // ---- update, staged (algo.hpp:651-666)
       Frag<D> out;
 #pragma unroll
       for (int t = 0; t < Frag<D>::N; ++t) out.v[t] = xi.v[t] + acc.v[t];
@@ -322,11 +349,11 @@ __global__ void __launch_bounds__(kPlainWarps * 32) plain_batch_kernel(const Pla
     }
   }
 
-  // Rows of the previous minibatch: staging buffer -> X.  Nothing in this
-  // launch reads those rows from X.
+  // Rows of minibatch j-1: staging buffer -> X.  Until the next launch passes
+  // its wait, every reader takes these rows from the staging buffer.
   for (int r = gw; r < a.prev_rows; r += total_w) {
     Frag<D> t;
-    load_nc(t, a.S_prev + size_t(r) * D, lane);
+    load_cg(t, a.S_prev + size_t(r) * D, lane);
     store<D, false>(t, a.X + size_t(a.prev_base + r) * D, lane);
   }
 

@@ -44,7 +44,7 @@ struct de_handle {
 
   // per-minibatch-size state
   Schedule sched;
-  float *d_stage[2] = {nullptr, nullptr};
+  float *d_stage = nullptr;  // three minibatch staging buffers
   size_t stage_cap = 0;
   float *d_parts = nullptr;
   size_t parts_cap = 0;
@@ -124,7 +124,7 @@ int grow_pinned(de_handle *h, T **p, size_t *cap, size_t need) {
   return DE_OK;
 }
 
-int default_edge_cap(int dim) { return dim >= 256 ? 32 : 64; }
+int default_edge_cap(int) { return kMaxEdgeCap; }
 
 // Work items of minibatch size B: each row of each minibatch becomes one item,
 // or ceil(deg / cap) items when its degree exceeds the cap.
@@ -182,7 +182,7 @@ void drop_graph(de_handle *h) {
 }
 
 int ensure_schedule(de_handle *h, int B) {
-  const int cap = h->opt.edge_cap > 0 ? h->opt.edge_cap : default_edge_cap(h->dim);
+  const int cap = h->opt.edge_cap > 0 ? std::min(h->opt.edge_cap, kMaxEdgeCap) : default_edge_cap(h->dim);
   if (h->sched.batch == B && h->sched.edge_cap == cap && h->sched.d_items) return DE_OK;
   drop_graph(h);
   if (h->sched.d_items) cudaFree(h->sched.d_items);
@@ -209,8 +209,10 @@ int capture_epoch(de_handle *h, int ns) {
   for (int j = 0; j < s.batches && err == cudaSuccess; ++j) {
     PlainBatchArgs a{};
     a.X = h->d_x;
-    a.S_prev = h->d_stage[(j + 1) & 1];
-    a.S_cur = h->d_stage[j & 1];
+    const size_t slice = size_t(s.batch) * h->dim;
+    a.S_cur = h->d_stage + slice * (j % 3);
+    a.S_prev = h->d_stage + slice * ((j + 2) % 3);
+    a.S_prev2 = h->d_stage + slice * ((j + 1) % 3);
     a.rowptr = h->d_rowptr;
     a.col = h->d_col;
     a.items = s.d_items + s.item_off[j];
@@ -219,6 +221,8 @@ int capture_epoch(de_handle *h, int ns) {
     a.rows = int32_t(std::min<int64_t>(s.batch, h->n - a.base));
     a.prev_base = j > 0 ? int32_t(int64_t(j - 1) * s.batch) : 0;
     a.prev_rows = j > 0 ? s.batch : 0;
+    a.prev2_base = j > 1 ? int32_t(int64_t(j - 2) * s.batch) : 0;
+    a.prev2_rows = j > 1 ? s.batch : 0;
     a.batch_id = j;
     a.batches = s.batches;
     a.last_batch_size = s.last_batch_size;
@@ -240,7 +244,7 @@ int capture_epoch(de_handle *h, int ns) {
   if (err == cudaSuccess) {
     FlushArgs f{};
     f.X = h->d_x;
-    f.S_last = h->d_stage[(s.batches - 1) & 1];
+    f.S_last = h->d_stage + size_t(s.batch) * h->dim * ((s.batches - 1) % 3);
     f.last_base = int32_t(int64_t(s.batches - 1) * s.batch);
     f.last_rows = s.last_batch_size;
     f.loss_partial = h->d_loss_partial;
@@ -359,8 +363,7 @@ int de_destroy(de_handle *h) {
   cudaFree(h->d_col);
   cudaFree(h->d_x);
   cudaFree(h->sched.d_items);
-  cudaFree(h->d_stage[0]);
-  cudaFree(h->d_stage[1]);
+  cudaFree(h->d_stage);
   cudaFree(h->d_parts);
   cudaFree(h->d_counters);
   cudaFree(h->d_loss_partial);
@@ -439,14 +442,7 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
   const Schedule &s = h->sched;
   bool moved = false;
   int rc = DE_OK;
-  const size_t rows_cap = size_t(s.batch) * h->dim;
-  if ((rc = grow(h, &h->d_stage[0], &h->stage_cap, rows_cap, &moved)) != DE_OK) return rc;
-  if (h->d_stage[1] == nullptr || moved) {
-    if (h->d_stage[1]) cudaFree(h->d_stage[1]);
-    h->d_stage[1] = nullptr;
-    DE_CUDA(h, cudaMalloc(&h->d_stage[1], h->stage_cap * sizeof(float)));
-    moved = true;
-  }
+  if ((rc = grow(h, &h->d_stage, &h->stage_cap, size_t(3) * s.batch * h->dim, &moved)) != DE_OK) return rc;
   bool counters_moved = false;
   if ((rc = grow(h, &h->d_parts, &h->parts_cap, size_t(std::max(s.max_parts, 1)) * h->dim, &moved)) ||
       (rc = grow(h, &h->d_counters, &h->counters_cap, size_t(std::max(s.max_split, 1)), &counters_moved)) ||

@@ -52,7 +52,7 @@ typedef struct de_options {
   int32_t device;       /* CUDA device ordinal                                         */
   void *stream;         /* cudaStream_t to run on; NULL: the handle creates its own    */
   double max_bound;     /* clip bound of every force component (reference: 5)          */
-  int32_t edge_cap;     /* max CSR entries per work item; 0 = automatic                */
+  int32_t edge_cap;     /* max CSR entries per work item (1..32); 0 = automatic        */
   int32_t pdl;          /* 1: overlap consecutive minibatch launches (programmatic     */
                         /*    dependent launch); 0: plain stream order                 */
   int32_t reserved[6];
