@@ -32,7 +32,7 @@ PRECISION = {"fp32": 0, "bf16": 1}
 # Every entry point include/distembed_gb300.h declares.
 EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings", "de_get_embeddings",
            "de_set_embeddings_f32", "de_get_embeddings_f32", "de_run", "de_run_from", "de_sync", "de_edge_updates",
-           "de_negatives", "de_stream", "de_last_error", "de_version")
+           "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version")
 
 
 class DEError(RuntimeError):
@@ -74,6 +74,8 @@ def lib():
         L.de_edge_updates.restype = _i64
         L.de_negatives.argtypes = [_i64, _i32, _i32, _vp]
         L.de_negatives.restype = None
+        L.de_minibatch_noalloc.argtypes = [_i64, _vp, _vp, _i32, _vp, _i32, _i32, _vp, _i32, _i32, _i32,
+                                           ctypes.c_float, ctypes.c_float, _vp, _vp]
         L.de_stream.argtypes = [_vp]
         L.de_stream.restype = _vp
         L.de_last_error.argtypes = [_vp]

@@ -27,6 +27,11 @@ namespace {
 thread_local std::string g_create_error;
 }
 
+namespace de {
+// Error text for entry points without a handle (read by de_last_error(NULL)).
+void set_thread_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace de
+
 struct de_handle {
   int64_t n = 0, nnz = 0;
   int dim = 0;

@@ -111,6 +111,26 @@ int64_t de_edge_updates(de_handle *h, int32_t first_epoch, int32_t epochs, int32
  * from minstd_rand(seed) (cpp/core/common.cpp:37-53), on the host. */
 void de_negatives(int64_t n, int32_t seed, int32_t ns, int64_t *out);
 
+/* One minibatch of the FP32 plain step on caller-owned device memory, allocating
+ * nothing.  No counterpart in the reference: it exists for callers that may not
+ * allocate device memory (a host framework that owns the device heap through its
+ * own pool, a latency-bound loop that cannot take cudaMalloc's implicit device
+ * synchronisation).  All pointers are device pointers: rowptr[n+1] and col (int32
+ * CSR), x (n x dim FP32, updated in place for rows of the minibatch), negs[ns]
+ * (this minibatch's draws), loss (nullable, one FP64: this minibatch's loss).
+ * rep_rows: leading rows of the minibatch that take the repulsive pass;
+ * skip_last_vertex: 1 drops edges into vertex n-1 as the reference does.  Work
+ * memory is a fixed device array of the library: batch rows * dim <= 1,048,576.
+ * Larger minibatches return DE_ERR_INVALID (text in de_last_error(NULL)).  The
+ * first call on a device looks that array up (cudaGetSymbolAddress), so make it
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race.  Launches on `stream` (a cudaStream_t, NULL = default stream) and
+ * returns without waiting. */
+int de_minibatch_noalloc(int64_t n, const int32_t *rowptr, const int32_t *col, int32_t dim, float *x,
+                         int32_t batch_id, int32_t batch_size, const int32_t *negs, int32_t ns,
+                         int32_t rep_rows, int32_t skip_last_vertex, float lr, float max_bound,
+                         double *loss, void *stream);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 
