@@ -1,0 +1,708 @@
+// BF16 precision form of the force-model SGD minibatch step (sm_103a).
+//
+// Storage: FP32 master copy Xm and a BF16 copy Xb of the embedding.  Every read
+// inside a minibatch uses Xb (FP32 arithmetic on BF16 values); the update goes to
+// Xm and is rounded back into Xb.  The minibatch's shared negatives (ns draws,
+// cpp/algo/algo.hpp:172-173) make the repulsive pass (algo.hpp:586-649) a dense
+// B x ns problem, done as two BF16 tcgen05 GEMMs per 128-row tile:
+//
+//   S  = X_tile . N^T                       (TMEM, FP32)
+//   r  = |x|^2 + |n|^2 - 2 S,  c = 2 / ((r + 1e-6)(1 + r))  -> C (BF16, SMEM)
+//   F += C . N                              (TMEM, FP32)
+//   repulsive force of row i = (sum_k c_ik) x_i - F_i
+//
+// The factorisation drops the per-component clip of algo.hpp:643, which is exact
+// when no component can reach the bound: |c (x_d - n_d)| <= c sqrt(r) < 5 for
+// r >= 0.25.  A pair with r < 0.25 (other than a row drawn as its own negative,
+// whose force is exactly zero) flags its row; flagged rows are recomputed pair by
+// pair in FP32 with the clip by bf16_fixup_kernel.
+//
+// Per minibatch: bf16_attract_kernel (attractive pass, warp per work item, plus
+// CTAs that gather the negatives into N / N^T), bf16_repulse_kernel (GEMMs and the
+// update of every unflagged row), bf16_fixup_kernel (flagged rows).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "de_device.cuh"
+#include "de_internal.h"
+
+namespace de {
+namespace {
+
+using namespace dev;
+
+constexpr float kNearR = 0.25f;   // below this squared distance a component may clip
+constexpr int kTileRows = 128;    // rows per tcgen05 tile (M)
+constexpr int kChunk = 64;        // negatives per GEMM chunk (one 128-B swizzle atom)
+constexpr long kSpinLimit = 1L << 22;
+
+// ------------------------------------------------------------ BF16 rows
+// Lane l holds components [l*N, l*N + N) of a row, N = dim / 32.
+
+template <int D>
+__device__ __forceinline__ void load_bf16_row(Frag<D> &f, const __nv_bfloat16 *row, int lane) {
+  constexpr int N = D / 32;
+  const __nv_bfloat16 *p = row + lane * N;
+  if constexpr (N == 8) {
+    uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float2 t = __bfloat1622float2(h[i]);
+      f.v[2 * i] = t.x;
+      f.v[2 * i + 1] = t.y;
+    }
+  } else if constexpr (N == 4) {
+    uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      float2 t = __bfloat1622float2(h[i]);
+      f.v[2 * i] = t.x;
+      f.v[2 * i + 1] = t.y;
+    }
+  } else {
+    static_assert(N == 2, "dim 64, 128 or 256");
+    unsigned u = __ldg(reinterpret_cast<const unsigned *>(p));
+    float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u));
+    f.v[0] = t.x;
+    f.v[1] = t.y;
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void store_f32_contig(const Frag<D> &f, float *row, int lane) {
+  constexpr int N = D / 32;
+  float *p = row + lane * N;
+#pragma unroll
+  for (int i = 0; i < N; i += 2) *reinterpret_cast<float2 *>(p + i) = make_float2(f.v[i], f.v[i + 1]);
+}
+
+// ------------------------------------------------------------ attractive + gather
+
+template <int D, int U>
+__device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
+                                                 int k, float lr, float bound, bool want_loss, double &loss,
+                                                 int lane) {
+  Frag<D> xn[U];
+  unsigned mask = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int n = __shfl_sync(kFull, ids, k + u);
+    if (n >= 0) {
+      load_bf16_row(xn[u], a.xb + size_t(n) * D, lane);
+      mask |= 1u << u;
+    } else {
+      xn[u] = xi;
+    }
+  }
+  if (mask) pair_forces<D, U, true>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
+}
+
+template <int D, int U>
+__global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF16BatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const bool want_loss = a.compute_loss != 0;
+  const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
+  const int epoch = a.epoch[0];
+  const float lr = a.lr[epoch];
+
+  if (int(blockIdx.x) >= item_ctas) {
+    // ---- gather the minibatch's negatives: N (k x dim), N^T (dim x k), |n|^2, ids
+    const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
+    const int gw = (blockIdx.x - item_ctas) * kPlainWarps + wib;
+    const int gws = (gridDim.x - item_ctas) * kPlainWarps;
+    if (gw == 0 && lane == 0) *a.flag_count = 0;
+    constexpr int N = D / 32;
+    for (int k = gw; k < a.kpad; k += gws) {
+      int n = k < a.ns ? __ldg(negs + k) : -1;
+      if (n >= a.n) n = -1;  // a draw equal to n contributes nothing
+      Frag<D> v;
+      if (n >= 0) load_bf16_row(v, a.xb + size_t(n) * D, lane);
+      else v.zero();
+      float sq = 0.f;
+#pragma unroll
+      for (int t = 0; t < N; ++t) {
+        const __nv_bfloat16 h = __float2bfloat16(v.v[t]);  // exact: v came from bf16
+        a.nb[size_t(k) * D + lane * N + t] = h;
+        a.nbt[size_t(lane * N + t) * a.kpad + k] = h;
+        sq = fmaf(v.v[t], v.v[t], sq);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
+      if (lane == 0) {
+        a.nn[k] = sq;
+        a.nid[k] = n;
+      }
+    }
+    return;
+  }
+
+  const int gw = blockIdx.x * kPlainWarps + wib;
+  if (gw >= a.n_items) return;
+  const WorkItem it = a.items[gw];
+  const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
+  const int cnt = it.e_end - it.e_begin;
+  int ids = -1;
+  if (lane < cnt) {
+    ids = __ldg(a.col + it.e_begin + lane);
+    if (ids == skip) ids = -1;
+  }
+  Frag<D> xi, acc;
+  load_bf16_row(xi, a.xb + size_t(a.base + it.row) * D, lane);
+  acc.zero();
+  double loss = 0.0;
+  for (int k = 0; k < cnt; k += U)
+    bf16_force_group<D, U>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
+
+  bool owner = true;
+  if (it.nparts > 1) {
+    const int P = it.nparts;
+    const int g = it.part / kCombineGroup;
+    const int ng = (P + kCombineGroup - 1) / kCombineGroup;
+    const int gsize = min(kCombineGroup, P - g * kCombineGroup);
+    store<D, true>(acc, a.P + size_t(it.first_slot + it.part) * D, lane);
+    owner = arrive_last(a.counters + it.counter + g, gsize, lane);
+    if (owner) {
+      sum_slots(acc, a.P + size_t(it.first_slot + g * kCombineGroup) * D, gsize, lane);
+      if (ng > 1) {
+        store<D, true>(acc, a.P + size_t(it.first_slot + P + g) * D, lane);
+        owner = arrive_last(a.counters + it.counter + ng, ng, lane);
+        if (owner) sum_slots(acc, a.P + size_t(it.first_slot + P) * D, ng, lane);
+      }
+    }
+  }
+  if (owner) store_f32_contig(acc, a.abuf + size_t(it.row) * D, lane);
+  if (want_loss) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kFull, loss, m);
+    if (lane == 0) a.loss_item[a.loss_off + gw] = loss;
+  }
+}
+
+// ------------------------------------------------------------ tcgen05 plumbing
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+// Shared-memory matrix descriptor: K-major operand in 128-byte swizzled atoms of
+// 8 rows x 128 B (stride between 8-row groups 1024 B), sm_100 descriptor version.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
+  return uint64_t((addr & 0x3FFFF) >> 4) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) |
+         (uint64_t(2) << 61);
+}
+
+// Instruction descriptor: BF16 x BF16 -> FP32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+// Waits for completion `parity` of the barrier; gives up after a bounded number
+// of polls, records the failure and returns false.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err_shared) {
+  for (long it = 0; it < kSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*reinterpret_cast<volatile int *>(err_shared)) return false;
+  }
+  *reinterpret_cast<volatile int *>(err_shared) = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,"
+      "%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ------------------------------------------------------------ repulsion GEMMs
+
+// Shared-memory plan of bf16_repulse_kernel (offsets from a 1024-aligned base).
+template <int D>
+struct RepulseSmem {
+  static constexpr int kAtoms = D / 64;                  // 128-B column atoms of a dim-wide row
+  static constexpr int kX = kAtoms * kTileRows * 128;    // X tile
+  static constexpr int kN = kAtoms * kChunk * 128;       // one chunk of N
+  static constexpr int kT = D * 128;                     // one chunk of N^T (D rows x 64 negatives)
+  static constexpr int kC = kTileRows * 128;             // one chunk of C (128 rows x 64 coefficients)
+  static constexpr int offX = 0;
+  static constexpr int offN = offX + kX;
+  static constexpr int offT = offN + 2 * kN;
+  static constexpr int offC = offT + 2 * kT;
+  static constexpr int bytes = offC + 2 * kC;
+  static constexpr int dynamic = bytes + 1024;           // + alignment slack
+};
+
+// Warp roles: 0-3 epilogue (thread t <-> tile row t <-> TMEM lane t), 4 TMA
+// producer, 5 MMA issuer and TMEM owner.  TMEM: S chunks in columns [0, 128)
+// (double buffered), F in columns [256, 256 + dim).
+template <int D>
+__global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_constant__ CUtensorMap map_x,
+                                                               const __grid_constant__ CUtensorMap map_n,
+                                                               const __grid_constant__ CUtensorMap map_t,
+                                                               const BF16BatchArgs a) {
+  using L = RepulseSmem<D>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t bar[18];
+  __shared__ uint32_t tmem_holder;
+  __shared__ int err;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nchunks = a.kpad / kChunk;
+  const int tile_base = blockIdx.x * kTileRows;  // row offset within the minibatch
+
+  // barrier ids
+  const uint32_t b0 = smem_u32(&bar[0]);
+  auto B = [&](int i) { return b0 + 8u * uint32_t(i); };
+  const int FULL_X = 0, FULL_N = 1, FULL_T = 3, FREE_N = 5, FREE_T = 7, S_FULL = 9, S_FREE = 11, C_FULL = 13,
+            C_FREE = 15, F_DONE = 17;
+  auto failed = [&]() { return *reinterpret_cast<volatile int *>(&err) != 0; };
+
+  if (tid == 0) {
+    err = 0;
+    mbar_init(B(FULL_X), 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(B(FULL_N + i), 1);
+      mbar_init(B(FULL_T + i), 1);
+      mbar_init(B(FREE_N + i), 1);
+      mbar_init(B(FREE_T + i), 1);
+      mbar_init(B(S_FULL + i), 1);
+      mbar_init(B(S_FREE + i), 128);
+      mbar_init(B(C_FULL + i), 128);
+      mbar_init(B(C_FREE + i), 1);
+    }
+    mbar_init(B(F_DONE), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_holder;
+  const uint32_t sX = smem_u32(sm + L::offX);
+  auto sN = [&](int b) { return smem_u32(sm + L::offN + b * L::kN); };
+  auto sT = [&](int b) { return smem_u32(sm + L::offT + b * L::kT); };
+  unsigned char *sC_ptr[2] = {sm + L::offC, sm + L::offC + L::kC};
+
+  if (warp == 4) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      int issued_n[2] = {0, 0}, issued_t[2] = {0, 0};
+      mbar_expect_tx(B(FULL_X), L::kX);
+      for (int ka = 0; ka < L::kAtoms; ++ka)
+        tma_load_2d(sX + ka * kTileRows * 128, &map_x, ka * 64, a.base + tile_base, B(FULL_X));
+      for (int c = 0; c < nchunks && !failed(); ++c) {
+        const int b = c & 1;
+        if (c >= 2 && !mbar_wait(B(FREE_N + b), ((c >> 1) + 1) & 1, &err)) break;
+        mbar_expect_tx(B(FULL_N + b), L::kN);
+        for (int ka = 0; ka < L::kAtoms; ++ka) tma_load_2d(sN(b) + ka * kChunk * 128, &map_n, ka * 64, c * kChunk, B(FULL_N + b));
+        ++issued_n[b];
+        if (c >= 2 && !mbar_wait(B(FREE_T + b), ((c >> 1) + 1) & 1, &err)) break;
+        mbar_expect_tx(B(FULL_T + b), L::kT);
+        tma_load_2d(sT(b), &map_t, c * kChunk, 0, B(FULL_T + b));
+        ++issued_t[b];
+      }
+      if (failed()) {
+        // bounded wait for every copy this thread started before the CTA leaves
+        int dummy = 0;
+        for (int b = 0; b < 2; ++b) {
+          if (issued_n[b]) mbar_wait(B(FULL_N + b), (issued_n[b] - 1) & 1, &dummy);
+          if (issued_t[b]) mbar_wait(B(FULL_T + b), (issued_t[b] - 1) & 1, &dummy);
+        }
+        mbar_wait(B(FULL_X), 0, &dummy);
+      }
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc1 = umma_idesc(kTileRows, kChunk);
+      constexpr uint32_t idesc2 = umma_idesc(kTileRows, D);
+      const uint32_t tmem_f = tmem + 256;
+      bool ok = mbar_wait(B(FULL_X), 0, &err);
+      auto gemm2 = [&](int c) {
+        const int b = c & 1;
+        if (!mbar_wait(B(C_FULL + b), (c >> 1) & 1, &err)) return false;
+        if (!mbar_wait(B(FULL_T + b), (c >> 1) & 1, &err)) return false;
+        tc_fence_after();
+        const uint32_t cbase = smem_u32(sC_ptr[b]);
+        for (int k = 0; k < kChunk / 16; ++k)
+          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc(sT(b) + k * 32), idesc2, (c > 0 || k > 0) ? 1u : 0u);
+        umma_commit(B(C_FREE + b));
+        umma_commit(B(FREE_T + b));
+        return true;
+      };
+      for (int c = 0; ok && c < nchunks; ++c) {
+        const int b = c & 1;
+        ok = mbar_wait(B(FULL_N + b), (c >> 1) & 1, &err);
+        if (ok && c >= 2) ok = mbar_wait(B(S_FREE + b), ((c >> 1) + 1) & 1, &err);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t tmem_s = tmem + uint32_t(b * kChunk);
+        for (int ka = 0; ka < L::kAtoms; ++ka)
+          for (int k = 0; k < 4; ++k)
+            umma(tmem_s, umma_desc(sX + ka * kTileRows * 128 + k * 32), umma_desc(sN(b) + ka * kChunk * 128 + k * 32),
+                 idesc1, (ka | k) ? 1u : 0u);
+        umma_commit(B(FREE_N + b));
+        umma_commit(B(S_FULL + b));
+        if (c >= 1) ok = gemm2(c - 1);
+      }
+      if (ok) ok = gemm2(nchunks - 1);
+      umma_commit(B(F_DONE));  // also fires after a failure, once issued MMAs finish
+      int dummy = 0;
+      mbar_wait(B(F_DONE), 0, &dummy);  // no tensor-core work may outlive the CTA
+    }
+  } else {
+    // ---------------- epilogue: thread t owns tile row t
+    const int t = tid;
+    const int epoch = a.epoch[0];
+    // rows that take the repulsive pass (algo.hpp:167-169, 594)
+    const int rep_rows = (a.quirks && epoch + a.epoch[1] > 0) ? a.last_batch_size : a.rows;
+    const int row_local = tile_base + t;
+    const bool row_valid = row_local < a.rows;
+    const bool rep_active = row_valid && row_local < rep_rows;
+    const int row_global = a.base + row_local;
+    const float lr = a.lr[epoch];
+    float xx = 0.f;
+    if (row_valid) {
+      const uint4 *xr = reinterpret_cast<const uint4 *>(a.xb + size_t(row_global) * D);
+      for (int i = 0; i < D / 8; ++i) {
+        uint4 u = __ldg(xr + i);
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+        for (int q = 0; q < 4; ++q) {
+          float2 f = __bfloat1622float2(h[q]);
+          xx = fmaf(f.x, f.x, fmaf(f.y, f.y, xx));
+        }
+      }
+    }
+    float rowsum = 0.f;
+    double loss = 0.0;
+    bool near = false;
+    const uint32_t lane_base = uint32_t(warp * 32) << 16;
+    for (int c = 0; c < nchunks; ++c) {
+      const int b = c & 1;
+      uint32_t s_raw[2][32] = {};
+      const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (c >> 1) & 1, &err));
+      tc_fence_after();
+      if (got) {
+        tmem_ld32(tmem + lane_base + uint32_t(b * kChunk), s_raw[0]);
+        tmem_ld32(tmem + lane_base + uint32_t(b * kChunk + 32), s_raw[1]);
+        tmem_wait_ld();
+      }
+      tc_fence_before();
+      mbar_arrive(B(S_FREE + b));
+      uint32_t packed[32];
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          float cv[2];
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int kk = c * kChunk + h * 32 + j + q;
+            const int nid = __ldg(a.nid + kk);
+            float cf = 0.f;
+            if (rep_active && nid >= 0) {
+              if (nid == row_global) {
+                loss += double(__logf(1.0f / 1e-6f));  // a row drawn as its own negative: no force
+              } else {
+                const float r = xx + __ldg(a.nn + kk) - 2.0f * __uint_as_float(s_raw[h][j + q]);
+                if (r < kNearR) {
+                  near = true;
+                } else {
+                  const float c2 = __fdividef(2.0f, (r + 1e-6f) * (1.0f + r));
+                  cf = __bfloat162float(__float2bfloat16(c2));
+                  loss += double(__logf(__fdividef(1.0f + r, r + 1e-6f)));
+                }
+              }
+            }
+            cv[q] = cf;
+            rowsum += cf;
+          }
+          __nv_bfloat162 p = __floats2bfloat162_rn(cv[0], cv[1]);
+          packed[h * 16 + j / 2] = *reinterpret_cast<uint32_t *>(&p);
+        }
+      if (c >= 2) mbar_wait(B(C_FREE + b), ((c >> 1) + 1) & 1, &err);
+      unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        *reinterpret_cast<uint4 *>(crow + ((j ^ (t & 7)) << 4)) =
+            make_uint4(packed[4 * j], packed[4 * j + 1], packed[4 * j + 2], packed[4 * j + 3]);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(B(C_FULL + b));
+    }
+    // every lane of a warp takes the same branch around the (warp-wide) TMEM loads
+    const bool done = __all_sync(kFull, mbar_wait(B(F_DONE), 0, &err) && !failed());
+    tc_fence_after();
+    if (row_valid && near && done) {
+      // recomputed pair by pair, with the clip, by bf16_fixup_kernel
+      const int slot = atomicAdd(a.flag_count, 1);
+      a.flag_rows[slot] = row_local;
+    }
+    const bool update = row_valid && !near && done;
+    float *xm = a.xm + size_t(row_global) * D;
+    __nv_bfloat16 *xb = a.xb + size_t(row_global) * D;
+    const float *ab = a.abuf + size_t(row_local) * D;
+    for (int d0 = 0; done && d0 < D; d0 += 32) {
+      uint32_t f[32];
+      tmem_ld32(tmem + lane_base + 256u + uint32_t(d0), f);
+      tmem_wait_ld();
+      if (update) {
+        for (int d = 0; d < 32; d += 8) {
+          uint4 xu = *reinterpret_cast<const uint4 *>(xb + d0 + d);
+          const __nv_bfloat162 *xh = reinterpret_cast<const __nv_bfloat162 *>(&xu);
+          float4 m0 = *reinterpret_cast<const float4 *>(xm + d0 + d);
+          float4 m1 = *reinterpret_cast<const float4 *>(xm + d0 + d + 4);
+          float4 a0 = *reinterpret_cast<const float4 *>(ab + d0 + d);
+          float4 a1 = *reinterpret_cast<const float4 *>(ab + d0 + d + 4);
+          float m[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+          const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+          uint32_t outp[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 xv = __bfloat1622float2(xh[q]);
+            const float f0 = rowsum * xv.x - __uint_as_float(f[d + 2 * q]);
+            const float f1 = rowsum * xv.y - __uint_as_float(f[d + 2 * q + 1]);
+            m[2 * q] += av[2 * q] + lr * f0;
+            m[2 * q + 1] += av[2 * q + 1] + lr * f1;
+            __nv_bfloat162 p = __floats2bfloat162_rn(m[2 * q], m[2 * q + 1]);
+            outp[q] = *reinterpret_cast<uint32_t *>(&p);
+          }
+          *reinterpret_cast<float4 *>(xm + d0 + d) = make_float4(m[0], m[1], m[2], m[3]);
+          *reinterpret_cast<float4 *>(xm + d0 + d + 4) = make_float4(m[4], m[5], m[6], m[7]);
+          *reinterpret_cast<uint4 *>(xb + d0 + d) = make_uint4(outp[0], outp[1], outp[2], outp[3]);
+        }
+      }
+    }
+    if (update) a.loss_row[row_global] = loss;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (failed() && tid == 0) atomicExch(a.err, 1);
+  if (warp == 5) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+}
+
+// ------------------------------------------------------------ exact rows
+
+// Flagged rows: the repulsive pass pair by pair in FP32 on the BF16 values, with
+// the per-component clip (algo.hpp:633-645), then the update.  One CTA per row,
+// warp w takes negatives w, w+8, ...; the warps' sums are added in warp order.
+template <int D>
+__global__ void __launch_bounds__(256) bf16_fixup_kernel(const BF16BatchArgs a) {
+  __shared__ float part[8][D];
+  __shared__ double part_loss[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int count = *a.flag_count;
+  const int epoch = a.epoch[0];
+  const float lr = a.lr[epoch];
+  for (int s = blockIdx.x; s < count; s += gridDim.x) {
+    const int row_local = a.flag_rows[s];
+    const int row = a.base + row_local;
+    Frag<D> xi, acc;
+    load_bf16_row(xi, a.xb + size_t(row) * D, lane);
+    acc.zero();
+    double loss = 0.0;
+    for (int k = w; k < a.kpad; k += 8) {
+      const int nid = __ldg(a.nid + k);
+      if (nid < 0) continue;
+      if (nid == row) {
+        if (lane == 0) loss += double(__logf(1.0f / 1e-6f));
+        continue;
+      }
+      Frag<D> xn;
+      load_bf16_row(xn, a.nb + size_t(k) * D, lane);
+      float diff[D / 32];
+      float p = 0.f;
+#pragma unroll
+      for (int t = 0; t < D / 32; ++t) {
+        diff[t] = xi.v[t] - xn.v[t];
+        p = fmaf(diff[t], diff[t], p);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
+      const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
+#pragma unroll
+      for (int t = 0; t < D / 32; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
+      if (lane == 0) loss += double(logf((1.0f + p) / (p + 1e-6f)));
+    }
+#pragma unroll
+    for (int t = 0; t < D / 32; ++t) part[w][lane * (D / 32) + t] = acc.v[t];
+    if (lane == 0) part_loss[w] = loss;
+    __syncthreads();
+    for (int d = threadIdx.x; d < D; d += 256) {
+      float r = 0.f;
+      for (int q = 0; q < 8; ++q) r += part[q][d];
+      const float m = a.xm[size_t(row) * D + d] + a.abuf[size_t(row_local) * D + d] + r;
+      a.xm[size_t(row) * D + d] = m;
+      a.xb[size_t(row) * D + d] = __float2bfloat16(m);
+    }
+    if (threadIdx.x == 0) {
+      double l = 0.0;
+      for (int q = 0; q < 8; ++q) l += part_loss[q];
+      a.loss_row[row] = l;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ epoch end
+
+__global__ void __launch_bounds__(256) bf16_flush_kernel(const BF16FlushArgs a) {
+  __shared__ double red[256];
+  __shared__ bool last;
+  double s = 0.0;
+  if (a.compute_loss) {
+    const int64_t total = a.n_items + a.n_rows;
+    const int64_t chunk = (total + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = blockIdx.x * chunk, hi = min(total, lo + chunk);
+    for (int64_t i = lo + threadIdx.x; i < hi; i += 256) s += i < a.n_items ? a.loss_item[i] : a.loss_row[i - a.n_items];
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    a.block_sums[blockIdx.x] = red[0];
+    __threadfence();
+    last = atomicAdd(a.done, 1) == int(gridDim.x) - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  s = 0.0;
+  for (int b = threadIdx.x; b < int(gridDim.x); b += 256) s += __ldcg(a.block_sums + b);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int e = a.epoch[0];
+    if (a.compute_loss) a.loss[e] = red[0];
+    a.epoch[0] = e + 1;
+    *a.done = 0;
+  }
+}
+
+__global__ void f32_to_bf16_kernel(const float *__restrict__ s, __nv_bfloat16 *__restrict__ d, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    d[i] = __float2bfloat16(s[i]);
+}
+
+}  // namespace
+
+int bf16_repulse_smem_bytes(int dim) {
+  switch (dim) {
+    case 64: return RepulseSmem<64>::dynamic;
+    case 128: return RepulseSmem<128>::dynamic;
+    case 256: return RepulseSmem<256>::dynamic;
+  }
+  return -1;
+}
+
+cudaError_t bf16_prepare(int dim) {
+  switch (dim) {
+    case 64: return cudaFuncSetAttribute(bf16_repulse_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<64>::dynamic);
+    case 128: return cudaFuncSetAttribute(bf16_repulse_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<128>::dynamic);
+    case 256: return cudaFuncSetAttribute(bf16_repulse_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<256>::dynamic);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
+                              const CUtensorMap &mt, cudaStream_t s) {
+  const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
+  const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps < 64 ? (a.kpad + kPlainWarps - 1) / kPlainWarps : 64;
+  const int tiles = (a.rows + kTileRows - 1) / kTileRows;
+  const int fix_ctas = 16;
+  switch (dim) {
+    case 64:
+      bf16_attract_kernel<64, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      bf16_repulse_kernel<64><<<tiles, 192, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_fixup_kernel<64><<<fix_ctas, 256, 0, s>>>(a);
+      break;
+    case 128:
+      bf16_attract_kernel<128, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      bf16_repulse_kernel<128><<<tiles, 192, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_fixup_kernel<128><<<fix_ctas, 256, 0, s>>>(a);
+      break;
+    case 256:
+      bf16_attract_kernel<256, 4><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      bf16_repulse_kernel<256><<<tiles, 192, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_fixup_kernel<256><<<fix_ctas, 256, 0, s>>>(a);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s) {
+  bf16_flush_kernel<<<kFlushBlocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  const int grid = int(count / 256 + 1 < 152 * 8 ? count / 256 + 1 : 152 * 8);
+  f32_to_bf16_kernel<<<grid, 256, 0, s>>>(src, dst, count);
+  return cudaGetLastError();
+}
+
+}  // namespace de

@@ -1,5 +1,7 @@
 // Internal types shared by the host runtime and the kernels.
 #pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -87,6 +89,55 @@ struct FlushArgs {
 };
 
 constexpr int kFlushBlocks = 152;
+
+// Kernel arguments of one minibatch of the BF16 precision form.
+struct BF16BatchArgs {
+  float *xm;                // [n, dim] FP32 master copy
+  __nv_bfloat16 *xb;        // [n, dim] BF16 copy, read by every force
+  const int32_t *rowptr, *col;
+  const WorkItem *items;
+  int32_t n_items;
+  int32_t base, rows, last_batch_size;  // minibatch rows; see rep_rows in the kernels
+  int32_t batch_id, batches;
+  int32_t n, quirks, compute_loss;
+  float bound;
+  const int32_t *negs;      // [epochs, batches, ns]
+  int32_t ns, kpad;         // kpad = ns rounded up to a multiple of 64 (>= 64)
+  const float *lr;          // [epochs]
+  const int32_t *epoch;     // device [2]
+  float *P;                 // partial slots of split rows
+  int32_t *counters;
+  float *abuf;              // [B, dim] attractive update of the minibatch (lr applied)
+  __nv_bfloat16 *nb;        // [kpad, dim] gathered negatives
+  __nv_bfloat16 *nbt;       // [dim, kpad] the same, transposed
+  float *nn;                // [kpad] squared norms of the gathered negatives
+  int32_t *nid;             // [kpad] vertex id of each negative, -1 = none
+  int32_t *flag_rows;       // [B] rows whose repulsion is recomputed exactly
+  int32_t *flag_count;
+  double *loss_item;        // attractive loss per work item of the epoch
+  int64_t loss_off;
+  double *loss_row;         // [n] repulsive loss per vertex of the epoch
+  int32_t *err;             // set when a bounded device wait gives up
+};
+
+struct BF16FlushArgs {
+  const double *loss_item;
+  const double *loss_row;
+  int64_t n_items, n_rows;
+  double *block_sums;
+  int32_t *done;
+  double *loss;
+  int32_t *epoch;
+  int32_t compute_loss;
+};
+
+// BF16 launchers (de_bf16.cu).
+int bf16_repulse_smem_bytes(int dim);
+cudaError_t bf16_prepare(int dim);
+cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
+                              const CUtensorMap &mt, cudaStream_t s);
+cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
+cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
 
 // Launchers (de_plain.cu).  pdl: launch with a programmatic dependency on the
 // previous kernel in the stream.

@@ -84,6 +84,24 @@ struct de_handle {
   // FP64 <-> FP32 staging for the host embedding copies
   double *d_stage64 = nullptr;
   size_t stage64_cap = 0;
+
+  // BF16 precision form: BF16 copy of the embedding (d_x is the FP32 master),
+  // per-minibatch buffers and the tensor maps of the GEMM operands
+  __nv_bfloat16 *d_xb = nullptr;
+  float *d_abuf = nullptr;
+  size_t abuf_cap = 0;
+  __nv_bfloat16 *d_nb = nullptr, *d_nbt = nullptr;
+  size_t nb_cap = 0;
+  float *d_nn = nullptr;
+  int32_t *d_nid = nullptr;
+  size_t kpad_cap = 0;
+  int32_t *d_flag_rows = nullptr;
+  size_t flag_cap = 0;
+  int32_t *d_flag_count = nullptr;
+  double *d_loss_row = nullptr;
+  int32_t *d_err = nullptr;
+  int kpad = 0;
+  CUtensorMap map_x{}, map_n{}, map_t{};
 };
 
 namespace {
@@ -206,7 +224,139 @@ void draw_negatives(int64_t n, int seed, int ns, int32_t *out) {
   for (int k = 0; k < ns; ++k) out[k] = dist(gen);
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 2-D BF16 tensor map over a row-major [rows, cols] array, box [box_rows, 64],
+// 128-byte swizzle (the layout the tcgen05 operand descriptors expect).
+int encode_map(de_handle *h, CUtensorMap *m, void *base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+  static EncodeTiledFn enc = nullptr;
+  if (!enc) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    DE_CUDA(h, cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (!fn) return fail(h, DE_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    enc = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(h, DE_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return DE_OK;
+}
+
+int capture_epoch_bf16(de_handle *h, int ns) {
+  const Schedule &s = h->sched;
+  cudaStream_t st = h->stream;
+  DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int j = 0; j < s.batches && err == cudaSuccess; ++j) {
+    BF16BatchArgs a{};
+    a.xm = h->d_x;
+    a.xb = h->d_xb;
+    a.rowptr = h->d_rowptr;
+    a.col = h->d_col;
+    a.items = s.d_items + s.item_off[j];
+    a.n_items = int32_t(s.item_off[j + 1] - s.item_off[j]);
+    a.base = int32_t(int64_t(j) * s.batch);
+    a.rows = int32_t(std::min<int64_t>(s.batch, h->n - a.base));
+    a.last_batch_size = s.last_batch_size;
+    a.batch_id = j;
+    a.batches = s.batches;
+    a.n = int32_t(h->n);
+    a.quirks = h->opt.ref_quirks;
+    a.compute_loss = h->opt.compute_loss;
+    a.bound = float(h->opt.max_bound);
+    a.negs = h->d_negs;
+    a.ns = ns;
+    a.kpad = h->kpad;
+    a.lr = h->d_lr;
+    a.epoch = h->d_epoch;
+    a.P = h->d_parts;
+    a.counters = h->d_counters;
+    a.abuf = h->d_abuf;
+    a.nb = h->d_nb;
+    a.nbt = h->d_nbt;
+    a.nn = h->d_nn;
+    a.nid = h->d_nid;
+    a.flag_rows = h->d_flag_rows;
+    a.flag_count = h->d_flag_count;
+    a.loss_item = h->d_loss_partial;
+    a.loss_off = s.item_off[j];
+    a.loss_row = h->d_loss_row;
+    a.err = h->d_err;
+    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st);
+  }
+  if (err == cudaSuccess) {
+    BF16FlushArgs f{};
+    f.loss_item = h->d_loss_partial;
+    f.loss_row = h->d_loss_row;
+    f.n_items = s.n_items;
+    f.n_rows = h->n;
+    f.block_sums = h->d_block_sums;
+    f.done = h->d_done;
+    f.loss = h->d_loss;
+    f.epoch = h->d_epoch;
+    f.compute_loss = h->opt.compute_loss;
+    err = launch_bf16_flush(f, st);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(st, &g);
+  if (err != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(h, err, "kernel launch during capture");
+  }
+  if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+  cudaError_t e3 = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e3 != cudaSuccess) {
+    h->graph = nullptr;
+    return cuda_fail(h, e3, "cudaGraphInstantiate");
+  }
+  h->graph_batch = s.batch;
+  h->graph_ns = ns;
+  return DE_OK;
+}
+
+// Buffers of the BF16 form for minibatch size B and ns negatives.
+int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
+  const Schedule &s = h->sched;
+  const int kpad = std::max(64, (ns + 63) / 64 * 64);
+  bool m = false;
+  int rc = DE_OK;
+  if ((rc = grow(h, &h->d_abuf, &h->abuf_cap, size_t(s.batch) * h->dim, &m)) ||
+      (rc = grow(h, &h->d_flag_rows, &h->flag_cap, size_t(s.batch), &m)))
+    return rc;
+  if (size_t(kpad) > h->kpad_cap || !h->d_nn) {
+    for (void *p : {static_cast<void *>(h->d_nn), static_cast<void *>(h->d_nid), static_cast<void *>(h->d_nb),
+                    static_cast<void *>(h->d_nbt)})
+      if (p) cudaFree(p);
+    h->d_nn = nullptr; h->d_nid = nullptr; h->d_nb = nullptr; h->d_nbt = nullptr;
+    DE_CUDA(h, cudaMalloc(&h->d_nn, kpad * sizeof(float)));
+    DE_CUDA(h, cudaMalloc(&h->d_nid, kpad * sizeof(int32_t)));
+    DE_CUDA(h, cudaMalloc(&h->d_nb, size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
+    DE_CUDA(h, cudaMalloc(&h->d_nbt, size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
+    h->kpad_cap = kpad;
+    m = true;
+  }
+  if (kpad != h->kpad || m) {
+    h->kpad = kpad;
+    if ((rc = encode_map(h, &h->map_x, h->d_xb, uint64_t(h->n), uint64_t(h->dim), 128)) ||
+        (rc = encode_map(h, &h->map_n, h->d_nb, uint64_t(kpad), uint64_t(h->dim), 64)) ||
+        (rc = encode_map(h, &h->map_t, h->d_nbt, uint64_t(h->dim), uint64_t(kpad), uint32_t(h->dim))))
+      return rc;
+    m = true;
+  }
+  if (m) *moved = true;
+  return DE_OK;
+}
+
 int capture_epoch(de_handle *h, int ns) {
+  if (h->opt.precision == DE_PRECISION_BF16) return capture_epoch_bf16(h, ns);
   const Schedule &s = h->sched;
   cudaStream_t st = h->stream;
   DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -279,6 +429,17 @@ int capture_epoch(de_handle *h, int ns) {
   return DE_OK;
 }
 
+// A kernel whose bounded wait gave up records it in d_err; report and re-arm.
+int check_device_error(de_handle *h) {
+  int32_t e = 0;
+  DE_CUDA(h, cudaMemcpy(&e, h->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (e) {
+    DE_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int32_t)));
+    return fail(h, DE_ERR_CUDA, "a device-side wait timed out; results of this call are not valid");
+  }
+  return DE_OK;
+}
+
 int check_csr(de_handle *h, int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz) {
   if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(h, DE_ERR_INVALID, "rowptr must start at 0 and end at nnz");
   for (int64_t i = 0; i < n; ++i)
@@ -315,8 +476,10 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
     return fail(nullptr, DE_ERR_UNSUPPORTED, "n and nnz must be below 2^31 - 1");
   auto h = std::make_unique<de_handle>();
   if (opts) h->opt = *opts; else de_default_options(&h->opt);
-  if (h->opt.precision != DE_PRECISION_FP32)
-    return fail(nullptr, DE_ERR_UNSUPPORTED, "precision not available in this build");
+  if (h->opt.precision != DE_PRECISION_FP32 && h->opt.precision != DE_PRECISION_BF16)
+    return fail(nullptr, DE_ERR_INVALID, "unknown precision");
+  if (h->opt.precision == DE_PRECISION_BF16 && dim < 64)
+    return fail(nullptr, DE_ERR_UNSUPPORTED, "the BF16 form needs dim 64, 128 or 256");
   if (!(h->opt.max_bound > 0)) return fail(nullptr, DE_ERR_INVALID, "max_bound must be positive");
   if (int rc = check_csr(h.get(), n, rowptr, col, nnz)) return fail(nullptr, rc, h->err);
   h->n = n;
@@ -347,14 +510,26 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
       (e = cudaMalloc(&h->d_epoch, 2 * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_block_sums, kFlushBlocks * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&h->d_done, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_err, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_flag_count, sizeof(int32_t))) != cudaSuccess ||
       (e = cudaHostAlloc(&h->h_epoch, 2 * sizeof(int32_t), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "allocation"));
   if ((e = cudaMemcpy(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (nnz > 0 && (e = cudaMemcpy(h->d_col, col32.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess) ||
       (e = cudaMemset(h->d_x, 0, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
-      (e = cudaMemset(h->d_done, 0, sizeof(int32_t))) != cudaSuccess)
+      (e = cudaMemset(h->d_done, 0, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMemset(h->d_err, 0, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMemset(h->d_flag_count, 0, sizeof(int32_t))) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "upload"));
+  if (h->opt.precision == DE_PRECISION_BF16) {
+    if ((e = cudaMalloc(&h->d_xb, size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_loss_row, size_t(n) * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemset(h->d_xb, 0, size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
+        (e = cudaMemset(h->d_loss_row, 0, size_t(n) * sizeof(double))) != cudaSuccess ||
+        (e = bf16_prepare(dim)) != cudaSuccess)
+      return bail(cuda_fail(h.get(), e, "BF16 form set-up"));
+  }
   *out = h.release();
   return DE_OK;
 }
@@ -374,6 +549,16 @@ int de_destroy(de_handle *h) {
   cudaFree(h->d_loss_partial);
   cudaFree(h->d_block_sums);
   cudaFree(h->d_done);
+  cudaFree(h->d_err);
+  cudaFree(h->d_flag_count);
+  cudaFree(h->d_xb);
+  cudaFree(h->d_abuf);
+  cudaFree(h->d_nb);
+  cudaFree(h->d_nbt);
+  cudaFree(h->d_nn);
+  cudaFree(h->d_nid);
+  cudaFree(h->d_flag_rows);
+  cudaFree(h->d_loss_row);
   cudaFree(h->d_epoch);
   cudaFree(h->d_loss);
   cudaFree(h->d_negs);
@@ -400,6 +585,7 @@ static int copy_embeddings_f64(de_handle *h, double *host, bool to_device) {
     if (to_device) {
       DE_CUDA(h, cudaMemcpyAsync(h->d_stage64, host + off, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
       DE_CUDA(h, launch_f64_to_f32(h->d_stage64, h->d_x + off, cnt, h->stream));
+      if (h->d_xb) DE_CUDA(h, launch_f32_to_bf16(h->d_x + off, h->d_xb + off, cnt, h->stream));
     } else {
       DE_CUDA(h, launch_f32_to_f64(h->d_x + off, h->d_stage64, cnt, h->stream));
       DE_CUDA(h, cudaMemcpyAsync(host + off, h->d_stage64, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -417,6 +603,7 @@ int de_set_embeddings_f32(de_handle *h, const float *x, int32_t on_device) {
   DE_CUDA(h, cudaSetDevice(h->device));
   DE_CUDA(h, cudaMemcpyAsync(h->d_x, x, size_t(h->n) * h->dim * sizeof(float),
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+  if (h->d_xb) DE_CUDA(h, launch_f32_to_bf16(h->d_x, h->d_xb, h->n * h->dim, h->stream));
   DE_CUDA(h, cudaStreamSynchronize(h->stream));
   return DE_OK;
 }
@@ -447,7 +634,9 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
   const Schedule &s = h->sched;
   bool moved = false;
   int rc = DE_OK;
-  if ((rc = grow(h, &h->d_stage, &h->stage_cap, size_t(3) * s.batch * h->dim, &moved)) != DE_OK) return rc;
+  const bool bf16 = h->opt.precision == DE_PRECISION_BF16;
+  if (!bf16 && (rc = grow(h, &h->d_stage, &h->stage_cap, size_t(3) * s.batch * h->dim, &moved)) != DE_OK) return rc;
+  if (bf16 && (rc = ensure_bf16_buffers(h, ns, &moved)) != DE_OK) return rc;
   bool counters_moved = false;
   if ((rc = grow(h, &h->d_parts, &h->parts_cap, size_t(std::max(s.max_parts, 1)) * h->dim, &moved)) ||
       (rc = grow(h, &h->d_counters, &h->counters_cap, size_t(std::max(s.max_split, 1)), &counters_moved)) ||
@@ -495,6 +684,7 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
     DE_CUDA(h, cudaMemcpyAsync(h->h_loss, h->d_loss, epochs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     DE_CUDA(h, cudaStreamSynchronize(h->stream));
     std::memcpy(loss_per_epoch, h->h_loss, epochs * sizeof(double));
+    if ((rc = check_device_error(h))) return rc;
   }
   DE_CUDA(h, cudaGetLastError());
   return DE_OK;
@@ -504,7 +694,7 @@ int de_sync(de_handle *h) {
   if (!h) return DE_ERR_INVALID;
   DE_CUDA(h, cudaSetDevice(h->device));
   DE_CUDA(h, cudaStreamSynchronize(h->stream));
-  return DE_OK;
+  return check_device_error(h);
 }
 
 int64_t de_edge_updates(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size,
