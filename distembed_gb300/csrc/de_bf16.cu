@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
   __syncthreads();
   if (failed() && tid == 0) atomicExch(a.err, 1);
   if (warp == 5) {
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
   }
