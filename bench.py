@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="max CSR entries per work item (0: automatic)")
+    p.add_argument("--form", default="plain", choices=["plain", "bf16"],
+                   help="plain: FP32 plain form on R-MAT s20 (default line); bf16: BF16 precision form vs the "
+                        "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives")
     return p.parse_args()
 
 
@@ -312,10 +315,73 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+W3 = dict(scale=22, edge_factor=16, seed=2, dim=256, batch=8192, ns=1024, lr=0.02, epochs=10, init_seed=0)
+WORKLOAD3 = "rmat22_ef16_d256_b8192_ns1024"
+
+
+def timed_job(h, E, B, ns, lr, stream, warmup):
+    """Runs `warmup` epochs, then one E-epoch job with CUDA events around each
+    epoch; returns (per-epoch ms, per-epoch FP64 loss of the job)."""
+    import torch
+    for k in range(warmup):
+        h.run(1, B, ns, lr, want_loss=False, first_epoch=k % E)
+    h.sync()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(E + 1)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for e in range(E):
+        h.run(1, B, ns, lr, want_loss=False, first_epoch=e)
+        ev[e + 1].record(stream)
+    h.sync()
+    torch.cuda.synchronize()
+    ms = [ev[e].elapsed_time(ev[e + 1]) for e in range(E)]
+    return ms
+
+
+def run_bf16_form(args):
+    """BF16 precision form against the FP32 plain form on the same 10-epoch job."""
+    import torch
+
+    import distembed_gb300 as de
+    from distembed_gb300 import graphgen as gg
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    n, rowptr, col = gg.rmat_csr(W3["scale"], W3["edge_factor"], seed=W3["seed"])
+    x0 = gg.init_embedding(n, W3["dim"], seed=W3["init_seed"]).astype(np.float32)
+    gen_s = time.perf_counter() - t0
+    dim, B, ns, lr, E = W3["dim"], W3["batch"], W3["ns"], W3["lr"], W3["epochs"]
+    out = {}
+    for form in ("fp32", "bf16"):
+        h = de.Handle(rowptr, col, dim, precision=form, quirks=True, compute_loss=True, pdl=bool(args.pdl))
+        stream = torch.cuda.ExternalStream(h.stream, device=0)
+        h.set_embeddings(x0)
+        upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
+        ms = timed_job(h, E, B, ns, lr, stream, warmup=1)
+        h.set_embeddings(x0)
+        loss = h.run(E, B, ns, lr, want_loss=True)   # the same job, for its losses
+        out[form] = {"edge_updates_per_s": sum(upd) / (sum(ms) / 1e3), "ms_per_epoch": statistics.mean(ms),
+                     "loss_per_epoch": [float(v) for v in loss]}
+        h.close()
+    gap = abs(out["bf16"]["loss_per_epoch"][-1] - out["fp32"]["loss_per_epoch"][-1]) / out["fp32"]["loss_per_epoch"][-1]
+    line = {"metric": METRIC, "value": out["bf16"]["edge_updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": E,
+            "warmup": 1, "ms_per_step": out["bf16"]["ms_per_epoch"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic: R-MAT scale 22 (ef 16, a.57 b.19 c.19, seed 2), U[-0.5,0.5] init (seed 0)",
+            "config": {"workload": WORKLOAD3 + "_bf16", "n": n, "nnz": int(len(col)), "dim": dim, "batch": B,
+                       "ns": ns, "lr": lr, "epochs_per_job": E, "step": "one epoch (512 minibatches)",
+                       "generate_s": round(gen_s, 1)},
+            "compare": {"fp32_plain": {k: v for k, v in out["fp32"].items()}, "bf16": out["bf16"],
+                        "bf16_over_fp32": out["bf16"]["edge_updates_per_s"] / out["fp32"]["edge_updates_per_s"],
+                        "final_loss_gap_vs_fp32": gap}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.form == "bf16":
+        run_bf16_form(args)
     else:
         run_ours(args)
 
