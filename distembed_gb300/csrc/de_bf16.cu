@@ -83,7 +83,7 @@ __device__ __forceinline__ void store_f32_contig(const Frag<D> &f, float *row, i
 
 template <int D, int U>
 __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
-                                                 int k, float lr, float bound, bool want_loss, double &loss,
+                                                 int k, float lr, float bound, bool want_loss, float &loss,
                                                  int lane) {
   Frag<D> xn[U];
   unsigned mask = 0;
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF
   Frag<D> xi, acc;
   load_bf16_row(xi, a.xb + size_t(a.base + it.row) * D, lane);
   acc.zero();
-  double loss = 0.0;
+  float loss = 0.f;  // this item's loss terms (FP32); the epoch sum is FP64
   for (int k = 0; k < cnt; k += U)
     bf16_force_group<D, U>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
 
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF
   if (want_loss) {
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kFull, loss, m);
-    if (lane == 0) a.loss_item[a.loss_off + gw] = loss;
+    if (lane == 0) a.loss_item[a.loss_off + gw] = double(loss);
   }
 }
 
@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
     float rowsum = 0.f;
     double loss = 0.0;
     bool near = false;
+    const float kSelfLoss = __logf(1.0f / 1e-6f);
     const uint32_t lane_base = uint32_t(warp * 32) << 16;
     for (int c = 0; c < nchunks; ++c) {
       const int b = c & 1;
@@ -441,37 +442,47 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
       }
       tc_fence_before();
       mbar_arrive(B(S_FREE + b));
+      // Loss terms of the chunk: the log of a product of eight ratios at a time
+      // (each ratio (1+r)/(r+1e-6) lies in [1, 5] here), summed in FP32, then
+      // folded into the row's FP64 total once per chunk.
       uint32_t packed[32];
+      float loss_c = 0.f;
 #pragma unroll
       for (int h = 0; h < 2; ++h)
 #pragma unroll
-        for (int j = 0; j < 32; j += 2) {
-          float cv[2];
+        for (int j = 0; j < 32; j += 8) {
+          float prod = 1.f;
+          float cv[8];
 #pragma unroll
-          for (int q = 0; q < 2; ++q) {
+          for (int q = 0; q < 8; ++q) {
             const int kk = c * kChunk + h * 32 + j + q;
             const int nid = __ldg(a.nid + kk);
             float cf = 0.f;
             if (rep_active && nid >= 0) {
               if (nid == row_global) {
-                loss += double(__logf(1.0f / 1e-6f));  // a row drawn as its own negative: no force
+                loss_c += kSelfLoss;  // a row drawn as its own negative: no force
               } else {
                 const float r = xx + __ldg(a.nn + kk) - 2.0f * __uint_as_float(s_raw[h][j + q]);
                 if (r < kNearR) {
                   near = true;
                 } else {
-                  const float c2 = __fdividef(2.0f, (r + 1e-6f) * (1.0f + r));
-                  cf = __bfloat162float(__float2bfloat16(c2));
-                  loss += double(__logf(__fdividef(1.0f + r, r + 1e-6f)));
+                  const float inv = __fdividef(1.0f, r + 1e-6f);
+                  cf = __bfloat162float(__float2bfloat16(2.0f * inv * __fdividef(1.0f, 1.0f + r)));
+                  prod *= (1.0f + r) * inv;
                 }
               }
             }
-            cv[q] = cf;
             rowsum += cf;
+            cv[q] = cf;
           }
-          __nv_bfloat162 p = __floats2bfloat162_rn(cv[0], cv[1]);
-          packed[h * 16 + j / 2] = *reinterpret_cast<uint32_t *>(&p);
+#pragma unroll
+          for (int q = 0; q < 8; q += 2) {
+            __nv_bfloat162 p2 = __floats2bfloat162_rn(cv[q], cv[q + 1]);
+            packed[(h * 32 + j + q) / 2] = *reinterpret_cast<uint32_t *>(&p2);
+          }
+          loss_c += __logf(prod);
         }
+      loss += double(loss_c);
       if (c >= 2) mbar_wait(B(C_FREE + b), ((c >> 1) + 1) & 1, &err);
       unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
@@ -555,12 +566,12 @@ __global__ void __launch_bounds__(256) bf16_fixup_kernel(const BF16BatchArgs a) 
     Frag<D> xi, acc;
     load_bf16_row(xi, a.xb + size_t(row) * D, lane);
     acc.zero();
-    double loss = 0.0;
+    float loss = 0.f;
     for (int k = w; k < a.kpad; k += 8) {
       const int nid = __ldg(a.nid + k);
       if (nid < 0) continue;
       if (nid == row) {
-        if (lane == 0) loss += double(__logf(1.0f / 1e-6f));
+        if (lane == 0) loss += __logf(1.0f / 1e-6f);
         continue;
       }
       Frag<D> xn;
@@ -577,11 +588,11 @@ __global__ void __launch_bounds__(256) bf16_fixup_kernel(const BF16BatchArgs a) 
       const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
 #pragma unroll
       for (int t = 0; t < D / 32; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
-      if (lane == 0) loss += double(logf((1.0f + p) / (p + 1e-6f)));
+      if (lane == 0) loss += logf((1.0f + p) / (p + 1e-6f));
     }
 #pragma unroll
     for (int t = 0; t < D / 32; ++t) part[w][lane * (D / 32) + t] = acc.v[t];
-    if (lane == 0) part_loss[w] = loss;
+    if (lane == 0) part_loss[w] = double(loss);
     __syncthreads();
     for (int d = threadIdx.x; d < D; d += 256) {
       float r = 0.f;

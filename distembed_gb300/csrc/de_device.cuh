@@ -130,11 +130,12 @@ __device__ __forceinline__ float multi_warp_sum(float (&p)[U], int lane) {
 // pair u counts (invalid pairs must carry xn[u] == xi).  Attractive:
 // c = -2/(1+r); repulsive: c = 2/((r+1e-6)(1+r)) (algo.hpp:573, 626/641).
 // Each component is clipped and accumulated in pair order.  The loss term of a
-// pair is added on the lane that holds its full sum.
+// pair is added on the lane that holds its full sum (FP32 within one work
+// item; the caller folds it into the FP64 epoch sum).
 template <int D, int U, bool kAttract>
 __device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, const Frag<D> (&xn)[U],
                                             unsigned valid_mask, float lr, float bound, bool want_loss,
-                                            double &loss, int lane) {
+                                            float &loss, int lane) {
   constexpr int L = Log2<U>::value;
   float diff[U][Frag<D>::N];
   float p[U];
@@ -153,7 +154,7 @@ __device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, con
   float c = kAttract ? -2.0f / (1.0f + r) : 2.0f / ((r + 1e-6f) * (1.0f + r));
   if (!valid) c = 0.f;
   if (want_loss && valid && (lane & ((32 >> L) - 1)) == 0)
-    loss += double(kAttract ? log1pf(r) : logf((1.0f + r) / (r + 1e-6f)));
+    loss += kAttract ? log1pf(r) : logf((1.0f + r) / (r + 1e-6f));
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const float cu = __shfl_sync(kFull, c, u << (5 - L));

@@ -52,7 +52,7 @@ __device__ __forceinline__ const float *row_ptr(const PlainBatchArgs &a, int n, 
 // none) and applies their forces.  Missing rows get xi (zero force).
 template <int D, int U, bool kAttract, bool kAfterWait>
 __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
-                                            int k, float lr, float bound, bool want_loss, double &loss,
+                                            int k, float lr, float bound, bool want_loss, float &loss,
                                             int lane) {
   Frag<D> xn[U];
   unsigned mask = 0;
@@ -73,7 +73,7 @@ __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &ac
 // Forces of the ids held by the warp's lanes (-1 = none), U at a time.
 template <int D, int U, bool kAttract, bool kAfterWait>
 __device__ __forceinline__ void force_lanes(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
-                                            int cnt, float lr, float bound, bool want_loss, double &loss,
+                                            int cnt, float lr, float bound, bool want_loss, float &loss,
                                             int lane) {
   for (int k = 0; k < cnt; k += U)
     force_group<D, U, kAttract, kAfterWait>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
   const bool repulse = has_item && it.part == 0 && it.row < rep_rows;
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
 
-  double loss = 0.0;
+  float loss = 0.f;  // this item's loss terms (FP32); the epoch sum is FP64
   Frag<D> xi, acc;
   acc.zero();
   if (has_item) {
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
   if (want_loss && has_item) {
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kFull, loss, m);
-    if (lane == 0) a.loss_partial[a.loss_off + gw] = loss;
+    if (lane == 0) a.loss_partial[a.loss_off + gw] = double(loss);
   }
 }
 
