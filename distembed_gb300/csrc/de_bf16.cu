@@ -279,11 +279,16 @@ struct RepulseSmem {
   static constexpr int dynamic = bytes + 1024;           // + alignment slack
 };
 
-// Warp roles: 0-3 epilogue (thread t <-> tile row t <-> TMEM lane t), 4 TMA
-// producer, 5 MMA issuer and TMEM owner.  TMEM: S chunks in columns [0, 128)
-// (double buffered), F in columns [256, 256 + dim).
+// Warp roles: 0-7 epilogue, 8 TMA producer, 9 MMA issuer and TMEM owner.
+// Epilogue warp w serves TMEM lane quadrant w % 4 (tile rows 32(w%4) .. +31) and
+// column half w / 4: 32 of the 64 coefficients of each chunk, and half of the
+// dims in the final update.  TMEM: S chunks in columns [0, 128) (double
+// buffered), F in columns [256, 256 + dim).
+constexpr int kEpiThreads = 256;
+constexpr int kRepulseThreads = kEpiThreads + 64;
+
 template <int D>
-__global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_constant__ CUtensorMap map_x,
+__global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const __grid_constant__ CUtensorMap map_x,
                                                                const __grid_constant__ CUtensorMap map_n,
                                                                const __grid_constant__ CUtensorMap map_t,
                                                                const BF16BatchArgs a) {
@@ -293,6 +298,7 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
   __shared__ __align__(8) uint64_t bar[18];
   __shared__ uint32_t tmem_holder;
   __shared__ int err;
+  __shared__ float2 negmeta[2][kChunk];  // (|n|^2, vertex id) of a chunk's negatives
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = a.kpad / kChunk;
   const int tile_base = blockIdx.x * kTileRows;  // row offset within the minibatch
@@ -313,14 +319,14 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
       mbar_init(B(FREE_N + i), 1);
       mbar_init(B(FREE_T + i), 1);
       mbar_init(B(S_FULL + i), 1);
-      mbar_init(B(S_FREE + i), 128);
-      mbar_init(B(C_FULL + i), 128);
+      mbar_init(B(S_FREE + i), kEpiThreads);
+      mbar_init(B(C_FULL + i), kEpiThreads);
       mbar_init(B(C_FREE + i), 1);
     }
     mbar_init(B(F_DONE), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
                  "r"(512)
                  : "memory");
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
   auto sT = [&](int b) { return smem_u32(sm + L::offT + b * L::kT); };
   unsigned char *sC_ptr[2] = {sm + L::offC, sm + L::offC + L::kC};
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---------------- TMA producer
     if (lane == 0) {
       int issued_n[2] = {0, 0}, issued_t[2] = {0, 0};
@@ -363,7 +369,7 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
         mbar_wait(B(FULL_X), 0, &dummy);
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---------------- MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc1 = umma_idesc(kTileRows, kChunk);
@@ -403,8 +409,9 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
       mbar_wait(B(F_DONE), 0, &dummy);  // no tensor-core work may outlive the CTA
     }
   } else {
-    // ---------------- epilogue: thread t owns tile row t
-    const int t = tid;
+    // ---------------- epilogue
+    const int q4 = warp & 3, hf = warp >> 2;  // lane quadrant, column half
+    const int t = q4 * 32 + lane;             // tile row = TMEM lane
     const int epoch = a.epoch[0];
     // rows that take the repulsive pass (algo.hpp:167-169, 594)
     const int rep_rows = (a.quirks && epoch + a.epoch[1] > 0) ? a.last_batch_size : a.rows;
@@ -413,10 +420,13 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
     const bool rep_active = row_valid && row_local < rep_rows;
     const int row_global = a.base + row_local;
     const float lr = a.lr[epoch];
+    auto epi_sync = []() { asm volatile("bar.sync 1, 256;" ::: "memory"); };
+
+    // |x|^2 of the row from its BF16 values, each half summing half the dims
     float xx = 0.f;
     if (row_valid) {
-      const uint4 *xr = reinterpret_cast<const uint4 *>(a.xb + size_t(row_global) * D);
-      for (int i = 0; i < D / 8; ++i) {
+      const uint4 *xr = reinterpret_cast<const uint4 *>(a.xb + size_t(row_global) * D + hf * (D / 2));
+      for (int i = 0; i < D / 16; ++i) {
         uint4 u = __ldg(xr + i);
         const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
         for (int q = 0; q < 4; ++q) {
@@ -425,69 +435,76 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
         }
       }
     }
-    float rowsum = 0.f;
+    // per-row exchange between the two column halves, in the C buffers while
+    // they are idle: before chunk 1 writes C[1], and after every GEMM is done
+    float *xx_part = reinterpret_cast<float *>(sC_ptr[1]);
+    xx_part[hf * kTileRows + t] = xx;
+    // |n|^2 and vertex id of the chunk's negatives, staged once per chunk
+    const int et = hf * 128 + t;  // 0..255
+    if (et < kChunk) negmeta[0][et] = make_float2(__ldg(a.nn + et), __int_as_float(__ldg(a.nid + et)));
+    epi_sync();
+    xx = xx_part[t] + xx_part[kTileRows + t];
+
+    float rowsum = 0.f, self_loss = 0.f;
     double loss = 0.0;
     bool near = false;
     const float kSelfLoss = __logf(1.0f / 1e-6f);
-    const uint32_t lane_base = uint32_t(warp * 32) << 16;
+    const uint32_t lane_base = uint32_t(q4 * 32) << 16;
     for (int c = 0; c < nchunks; ++c) {
       const int b = c & 1;
-      uint32_t s_raw[2][32] = {};
+      if (c > 0) epi_sync();  // meta of chunk c visible; everyone is done with chunk c-1
+      if (c + 1 < nchunks && et < kChunk) {
+        const int kk = (c + 1) * kChunk + et;
+        negmeta[b ^ 1][et] = make_float2(__ldg(a.nn + kk), __int_as_float(__ldg(a.nid + kk)));
+      }
+      uint32_t s_raw[32] = {};
       const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (c >> 1) & 1, &err));
       tc_fence_after();
       if (got) {
-        tmem_ld32(tmem + lane_base + uint32_t(b * kChunk), s_raw[0]);
-        tmem_ld32(tmem + lane_base + uint32_t(b * kChunk + 32), s_raw[1]);
+        tmem_ld32(tmem + lane_base + uint32_t(b * kChunk + hf * 32), s_raw);
         tmem_wait_ld();
       }
       tc_fence_before();
       mbar_arrive(B(S_FREE + b));
-      // Loss terms of the chunk: the log of a product of eight ratios at a time
-      // (each ratio (1+r)/(r+1e-6) lies in [1, 5] here), summed in FP32, then
-      // folded into the row's FP64 total once per chunk.
-      uint32_t packed[32];
+      // Coefficients without branches, so the 32 pairs' chains interleave.
+      // Loss terms: the log of a product of eight ratios (each (1+r)/(r+1e-6)
+      // in [1, 5] for the pairs taken), summed in FP32, folded into FP64 once.
+      uint32_t packed[16];
       float loss_c = 0.f;
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
+      for (int j = 0; j < 32; j += 8) {
+        float prod = 1.f;
+        float cv[8];
 #pragma unroll
-        for (int j = 0; j < 32; j += 8) {
-          float prod = 1.f;
-          float cv[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int kk = c * kChunk + h * 32 + j + q;
-            const int nid = __ldg(a.nid + kk);
-            float cf = 0.f;
-            if (rep_active && nid >= 0) {
-              if (nid == row_global) {
-                loss_c += kSelfLoss;  // a row drawn as its own negative: no force
-              } else {
-                const float r = xx + __ldg(a.nn + kk) - 2.0f * __uint_as_float(s_raw[h][j + q]);
-                if (r < kNearR) {
-                  near = true;
-                } else {
-                  const float inv = __fdividef(1.0f, r + 1e-6f);
-                  cf = __bfloat162float(__float2bfloat16(2.0f * inv * __fdividef(1.0f, 1.0f + r)));
-                  prod *= (1.0f + r) * inv;
-                }
-              }
-            }
-            rowsum += cf;
-            cv[q] = cf;
-          }
-#pragma unroll
-          for (int q = 0; q < 8; q += 2) {
-            __nv_bfloat162 p2 = __floats2bfloat162_rn(cv[q], cv[q + 1]);
-            packed[(h * 32 + j + q) / 2] = *reinterpret_cast<uint32_t *>(&p2);
-          }
-          loss_c += __logf(prod);
+        for (int q = 0; q < 8; ++q) {
+          const float2 m = negmeta[b][hf * 32 + j + q];
+          const int nid = __float_as_int(m.y);
+          const bool self = nid == row_global;
+          const bool valid = rep_active && nid >= 0 && !self;
+          const float r = xx + m.x - 2.0f * __uint_as_float(s_raw[j + q]);
+          const bool nearp = valid && r < kNearR;
+          const bool use = valid && !nearp;
+          const float inv = __fdividef(1.0f, r + 1e-6f);
+          const float cc = __bfloat162float(__float2bfloat16(2.0f * inv * __fdividef(1.0f, 1.0f + r)));
+          cv[q] = use ? cc : 0.f;
+          prod *= use ? (1.0f + r) * inv : 1.0f;
+          self_loss += (rep_active && self) ? kSelfLoss : 0.f;
+          near |= nearp;
+          rowsum += cv[q];
         }
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+          __nv_bfloat162 p2 = __floats2bfloat162_rn(cv[q], cv[q + 1]);
+          packed[(j + q) / 2] = *reinterpret_cast<uint32_t *>(&p2);
+        }
+        loss_c += __logf(prod);
+      }
       loss += double(loss_c);
       if (c >= 2) mbar_wait(B(C_FREE + b), ((c >> 1) + 1) & 1, &err);
       unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        *reinterpret_cast<uint4 *>(crow + ((j ^ (t & 7)) << 4)) =
+      for (int j = 0; j < 4; ++j)
+        *reinterpret_cast<uint4 *>(crow + (((hf * 4 + j) ^ (t & 7)) << 4)) =
             make_uint4(packed[4 * j], packed[4 * j + 1], packed[4 * j + 2], packed[4 * j + 3]);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(B(C_FULL + b));
@@ -495,20 +512,34 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
     // every lane of a warp takes the same branch around the (warp-wide) TMEM loads
     const bool done = __all_sync(kFull, mbar_wait(B(F_DONE), 0, &err) && !failed());
     tc_fence_after();
-    if (row_valid && near && done) {
+    // combine the two column halves of each row
+    loss += double(self_loss);
+    float *rs_part = reinterpret_cast<float *>(sC_ptr[0]);
+    double *loss_part = reinterpret_cast<double *>(sC_ptr[0] + 1024);
+    int *near_part = reinterpret_cast<int *>(sC_ptr[0] + 3072);
+    rs_part[hf * kTileRows + t] = rowsum;
+    loss_part[hf * kTileRows + t] = loss;
+    near_part[hf * kTileRows + t] = near ? 1 : 0;
+    epi_sync();
+    rowsum = rs_part[t] + rs_part[kTileRows + t];
+    loss = loss_part[t] + loss_part[kTileRows + t];
+    near = (near_part[t] | near_part[kTileRows + t]) != 0;
+    if (hf == 0 && row_valid && near && done) {
       // recomputed pair by pair, with the clip, by bf16_fixup_kernel
       const int slot = atomicAdd(a.flag_count, 1);
       a.flag_rows[slot] = row_local;
     }
     const bool update = row_valid && !near && done;
-    float *xm = a.xm + size_t(row_global) * D;
-    __nv_bfloat16 *xb = a.xb + size_t(row_global) * D;
-    const float *ab = a.abuf + size_t(row_local) * D;
-    for (int d0 = 0; done && d0 < D; d0 += 32) {
+    const int dlo = hf * (D / 2);
+    float *xm = a.xm + size_t(row_global) * D + dlo;
+    __nv_bfloat16 *xb = a.xb + size_t(row_global) * D + dlo;
+    const float *ab = a.abuf + size_t(row_local) * D + dlo;
+    for (int d0 = 0; done && d0 < D / 2; d0 += 32) {
       uint32_t f[32];
-      tmem_ld32(tmem + lane_base + 256u + uint32_t(d0), f);
+      tmem_ld32(tmem + lane_base + 256u + uint32_t(dlo + d0), f);
       tmem_wait_ld();
       if (update) {
+#pragma unroll
         for (int d = 0; d < 32; d += 8) {
           uint4 xu = *reinterpret_cast<const uint4 *>(xb + d0 + d);
           const __nv_bfloat162 *xh = reinterpret_cast<const __nv_bfloat162 *>(&xu);
@@ -535,12 +566,12 @@ __global__ void __launch_bounds__(192, 1) bf16_repulse_kernel(const __grid_const
         }
       }
     }
-    if (update) a.loss_row[row_global] = loss;
+    if (hf == 0 && update) a.loss_row[row_global] = loss;
   }
   tc_fence_before();
   __syncthreads();
   if (failed() && tid == 0) atomicExch(a.err, 1);
-  if (warp == 5) {
+  if (warp == 9) {
     __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
@@ -686,17 +717,17 @@ cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap
   switch (dim) {
     case 64:
       bf16_attract_kernel<64, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<64><<<tiles, 192, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_repulse_kernel<64><<<tiles, kRepulseThreads, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
       bf16_fixup_kernel<64><<<fix_ctas, 256, 0, s>>>(a);
       break;
     case 128:
       bf16_attract_kernel<128, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<128><<<tiles, 192, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_repulse_kernel<128><<<tiles, kRepulseThreads, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
       bf16_fixup_kernel<128><<<fix_ctas, 256, 0, s>>>(a);
       break;
     case 256:
       bf16_attract_kernel<256, 4><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<256><<<tiles, 192, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
+      bf16_repulse_kernel<256><<<tiles, kRepulseThreads, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
       bf16_fixup_kernel<256><<<fix_ctas, 256, 0, s>>>(a);
       break;
     default:
