@@ -253,6 +253,10 @@ def run_ours(args):
     alg_epoch = algorithmic_bytes_per_epoch(n, nnz_eff, batches, dim, ns)
     mean_epoch_s = statistics.mean(step_ms) / 1e3
     achieved = alg_epoch / mean_epoch_s / 1e9
+    # one extra epoch with an event around every launch (no overlap between launches)
+    pms, kind = h.profile_epoch(B, ns, lr, first_epoch=0)
+    launch_us = float(pms[kind == 0].mean()) * 1e3
+    serial_achieved = alg_epoch / (float(pms[kind == 0].sum()) / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = profile_traffic()
 
@@ -303,7 +307,8 @@ def run_ours(args):
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "kernel": "plain_batch_kernel<128>",
                          "algorithmic_bytes_per_epoch": alg_epoch,
-                         "note": "achieved = algorithmic bytes / epoch time over 256 launches (gaps included)"},
+                         "note": "achieved = algorithmic bytes / epoch time over 256 launches (gaps included)",
+                         "launch_us_serial": launch_us, "achieved_serial_launches": serial_achieved},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": args.steps * (batches + 1),
@@ -359,8 +364,11 @@ def run_bf16_form(args):
         ms = timed_job(h, E, B, ns, lr, stream, warmup=1)
         h.set_embeddings(x0)
         loss = h.run(E, B, ns, lr, want_loss=True)   # the same job, for its losses
+        pms, kind = h.profile_epoch(B, ns, lr)      # one more epoch, an event around every launch
+        names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "exact_rows", 3: "flush"}
         out[form] = {"edge_updates_per_s": sum(upd) / (sum(ms) / 1e3), "ms_per_epoch": statistics.mean(ms),
-                     "loss_per_epoch": [float(v) for v in loss]}
+                     "loss_per_epoch": [float(v) for v in loss],
+                     "profiled_epoch_ms": {names[k]: round(float(pms[kind == k].sum()), 3) for k in sorted(set(kind.tolist()))}}
         h.close()
     gap = abs(out["bf16"]["loss_per_epoch"][-1] - out["fp32"]["loss_per_epoch"][-1]) / out["fp32"]["loss_per_epoch"][-1]
     line = {"metric": METRIC, "value": out["bf16"]["edge_updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": E,

@@ -31,7 +31,8 @@ PRECISION = {"fp32": 0, "bf16": 1}
 
 # Every entry point include/distembed_gb300.h declares.
 EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings", "de_get_embeddings",
-           "de_set_embeddings_f32", "de_get_embeddings_f32", "de_run", "de_run_from", "de_sync", "de_edge_updates",
+           "de_set_embeddings_f32", "de_get_embeddings_f32", "de_run", "de_run_from", "de_profile_epoch", "de_sync",
+           "de_edge_updates",
            "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version")
 
 
@@ -69,6 +70,7 @@ def lib():
         L.de_get_embeddings_f32.argtypes = [_vp, _vp, _i32]
         L.de_run.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp]
         L.de_run_from.argtypes = [_vp, _i32, _i32, _i32, _i32, _vp, _vp]
+        L.de_profile_epoch.argtypes = [_vp, _i32, _i32, _i32, ctypes.c_double, _vp, _vp, _i32, _vp]
         L.de_sync.argtypes = [_vp]
         L.de_edge_updates.argtypes = [_vp, _i32, _i32, _i32, _i32]
         L.de_edge_updates.restype = _i64
@@ -171,6 +173,17 @@ class Handle:
 
     def sync(self):
         self._check(lib().de_sync(self._h))
+
+    def profile_epoch(self, batch_size: int, ns: int, lr: float, first_epoch: int = 0):
+        """One epoch with a CUDA event around every launch; returns (ms[], kind[])
+        (kinds: 0 minibatch/attractive kernel, 1 repulsion GEMM, 2 exact rows, 3 flush)."""
+        count = ctypes.c_int32(0)
+        cap = 4 * (self.n // max(batch_size, 1) + 2) + 8
+        ms = np.zeros(cap, dtype=np.float32)
+        kind = np.zeros(cap, dtype=np.int32)
+        self._check(lib().de_profile_epoch(self._h, first_epoch, batch_size, ns, lr, ms.ctypes.data,
+                                           kind.ctypes.data, cap, ctypes.byref(count)))
+        return ms[:count.value], kind[:count.value]
 
     def edge_updates(self, epochs: int, batch_size: int, ns: int, first_epoch: int = 0) -> int:
         return int(lib().de_edge_updates(self._h, first_epoch, epochs, batch_size, ns))

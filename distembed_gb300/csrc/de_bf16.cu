@@ -709,26 +709,29 @@ cudaError_t bf16_prepare(int dim) {
 }
 
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s) {
+                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev) {
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
   const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps < 64 ? (a.kpad + kPlainWarps - 1) / kPlainWarps : 64;
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
   const int fix_ctas = 16;
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], s);
+  };
   switch (dim) {
     case 64:
-      bf16_attract_kernel<64, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<64><<<tiles, kRepulseThreads, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
-      bf16_fixup_kernel<64><<<fix_ctas, 256, 0, s>>>(a);
+      mark(0); bf16_attract_kernel<64, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      mark(1); bf16_repulse_kernel<64><<<tiles, kRepulseThreads, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
+      mark(2); bf16_fixup_kernel<64><<<fix_ctas, 256, 0, s>>>(a);
       break;
     case 128:
-      bf16_attract_kernel<128, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<128><<<tiles, kRepulseThreads, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
-      bf16_fixup_kernel<128><<<fix_ctas, 256, 0, s>>>(a);
+      mark(0); bf16_attract_kernel<128, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      mark(1); bf16_repulse_kernel<128><<<tiles, kRepulseThreads, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
+      mark(2); bf16_fixup_kernel<128><<<fix_ctas, 256, 0, s>>>(a);
       break;
     case 256:
-      bf16_attract_kernel<256, 4><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      bf16_repulse_kernel<256><<<tiles, kRepulseThreads, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
-      bf16_fixup_kernel<256><<<fix_ctas, 256, 0, s>>>(a);
+      mark(0); bf16_attract_kernel<256, 4><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+      mark(1); bf16_repulse_kernel<256><<<tiles, kRepulseThreads, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
+      mark(2); bf16_fixup_kernel<256><<<fix_ctas, 256, 0, s>>>(a);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -134,8 +134,10 @@ struct BF16FlushArgs {
 // BF16 launchers (de_bf16.cu).
 int bf16_repulse_smem_bytes(int dim);
 cudaError_t bf16_prepare(int dim);
+// ev (nullable): three events recorded before the attractive, repulsive and
+// exact-row launches of the minibatch.
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s);
+                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev);
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
 cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
 

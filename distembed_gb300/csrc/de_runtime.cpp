@@ -249,10 +249,10 @@ int encode_map(de_handle *h, CUtensorMap *m, void *base, uint64_t rows, uint64_t
   return DE_OK;
 }
 
-int capture_epoch_bf16(de_handle *h, int ns) {
+// Enqueues one epoch of the BF16 form on st.  ev (nullable): 3 events per
+// minibatch (before each of its launches) and one before the flush.
+cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_t *ev) {
   const Schedule &s = h->sched;
-  cudaStream_t st = h->stream;
-  DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int j = 0; j < s.batches && err == cudaSuccess; ++j) {
     BF16BatchArgs a{};
@@ -289,7 +289,7 @@ int capture_epoch_bf16(de_handle *h, int ns) {
     a.loss_off = s.item_off[j];
     a.loss_row = h->d_loss_row;
     a.err = h->d_err;
-    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st);
+    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st, ev ? ev + 3 * j : nullptr);
   }
   if (err == cudaSuccess) {
     BF16FlushArgs f{};
@@ -302,24 +302,10 @@ int capture_epoch_bf16(de_handle *h, int ns) {
     f.loss = h->d_loss;
     f.epoch = h->d_epoch;
     f.compute_loss = h->opt.compute_loss;
+    if (ev) cudaEventRecord(ev[3 * s.batches], st);
     err = launch_bf16_flush(f, st);
   }
-  cudaGraph_t g = nullptr;
-  cudaError_t e2 = cudaStreamEndCapture(st, &g);
-  if (err != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
-    return cuda_fail(h, err, "kernel launch during capture");
-  }
-  if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
-  cudaError_t e3 = cudaGraphInstantiate(&h->graph, g, 0);
-  cudaGraphDestroy(g);
-  if (e3 != cudaSuccess) {
-    h->graph = nullptr;
-    return cuda_fail(h, e3, "cudaGraphInstantiate");
-  }
-  h->graph_batch = s.batch;
-  h->graph_ns = ns;
-  return DE_OK;
+  return err;
 }
 
 // Buffers of the BF16 form for minibatch size B and ns negatives.
@@ -355,11 +341,11 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
   return DE_OK;
 }
 
-int capture_epoch(de_handle *h, int ns) {
-  if (h->opt.precision == DE_PRECISION_BF16) return capture_epoch_bf16(h, ns);
+// Enqueues one epoch of the FP32 plain form on st.  ev (nullable): one event
+// before each minibatch launch and one before the flush (the events also stop
+// launches from overlapping).
+cudaError_t enqueue_epoch_plain(de_handle *h, int ns, cudaStream_t st, cudaEvent_t *ev) {
   const Schedule &s = h->sched;
-  cudaStream_t st = h->stream;
-  DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int j = 0; j < s.batches && err == cudaSuccess; ++j) {
     PlainBatchArgs a{};
@@ -394,7 +380,8 @@ int capture_epoch(de_handle *h, int ns) {
     a.loss_off = s.item_off[j];
     a.epoch = h->d_epoch;
     const int grid = int(s.cta_off[j + 1] - s.cta_off[j]);
-    err = launch_plain_batch(h->dim, a, grid, h->opt.pdl && j > 0, st);
+    if (ev) cudaEventRecord(ev[j], st);
+    err = launch_plain_batch(h->dim, a, grid, h->opt.pdl && j > 0 && !ev, st);
   }
   if (err == cudaSuccess) {
     FlushArgs f{};
@@ -409,8 +396,34 @@ int capture_epoch(de_handle *h, int ns) {
     f.loss = h->d_loss;
     f.epoch = h->d_epoch;
     f.compute_loss = h->opt.compute_loss;
-    err = launch_flush(h->dim, f, h->opt.pdl != 0, st);
+    if (ev) cudaEventRecord(ev[s.batches], st);
+    err = launch_flush(h->dim, f, h->opt.pdl != 0 && !ev, st);
   }
+  return err;
+}
+
+// Launches of one epoch and the kind of each: 0 minibatch kernel (FP32) or
+// attractive kernel (BF16), 1 repulsive GEMM kernel, 2 exact-row kernel, 3 flush.
+std::vector<int> epoch_launch_kinds(const de_handle *h) {
+  std::vector<int> k;
+  if (h->opt.precision == DE_PRECISION_BF16)
+    for (int j = 0; j < h->sched.batches; ++j) k.insert(k.end(), {0, 1, 2});
+  else
+    k.assign(h->sched.batches, 0);
+  k.push_back(3);
+  return k;
+}
+
+cudaError_t enqueue_epoch(de_handle *h, int ns, cudaStream_t st, cudaEvent_t *ev) {
+  return h->opt.precision == DE_PRECISION_BF16 ? enqueue_epoch_bf16(h, ns, st, ev)
+                                               : enqueue_epoch_plain(h, ns, st, ev);
+}
+
+int capture_epoch(de_handle *h, int ns) {
+  const Schedule &s = h->sched;
+  cudaStream_t st = h->stream;
+  DE_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t err = enqueue_epoch(h, ns, st, nullptr);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(st, &g);
   if (err != cudaSuccess) {
@@ -622,13 +635,10 @@ int de_run(de_handle *h, int32_t epochs, int32_t batch_size, int32_t ns, const d
   return de_run_from(h, 0, epochs, batch_size, ns, lr_per_epoch, loss_per_epoch);
 }
 
-int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
-                const double *lr_per_epoch, double *loss_per_epoch) {
-  if (!h) return DE_ERR_INVALID;
-  if (first_epoch < 0 || epochs < 0 || batch_size <= 0 || ns < 0)
-    return fail(h, DE_ERR_INVALID, "first_epoch >= 0, epochs >= 0, batch_size > 0, ns >= 0");
-  if (epochs > 0 && !lr_per_epoch) return fail(h, DE_ERR_INVALID, "lr_per_epoch is NULL");
-  if (epochs == 0) return DE_OK;
+// Schedule, buffers and per-call uploads (negatives, learning rates, epoch
+// counter) for `epochs` epochs starting at first_epoch; arguments already checked.
+static int prepare_run(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
+                       const double *lr_per_epoch) {
   DE_CUDA(h, cudaSetDevice(h->device));
   if (int rc = ensure_schedule(h, batch_size)) return rc;
   const Schedule &s = h->sched;
@@ -674,7 +684,19 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
   h->h_epoch[0] = 0;
   h->h_epoch[1] = first_epoch;
   DE_CUDA(h, cudaMemcpyAsync(h->d_epoch, h->h_epoch, 2 * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  return DE_OK;
+}
 
+int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
+                const double *lr_per_epoch, double *loss_per_epoch) {
+  if (!h) return DE_ERR_INVALID;
+  if (first_epoch < 0 || epochs < 0 || batch_size <= 0 || ns < 0)
+    return fail(h, DE_ERR_INVALID, "first_epoch >= 0, epochs >= 0, batch_size > 0, ns >= 0");
+  if (epochs > 0 && !lr_per_epoch) return fail(h, DE_ERR_INVALID, "lr_per_epoch is NULL");
+  if (epochs == 0) return DE_OK;
+  int rc = prepare_run(h, first_epoch, epochs, batch_size, ns, lr_per_epoch);
+  if (rc) return rc;
+  const Schedule &s = h->sched;
   if (!h->graph || h->graph_batch != s.batch || h->graph_ns != ns) {
     drop_graph(h);
     if ((rc = capture_epoch(h, ns))) return rc;
@@ -694,6 +716,30 @@ int de_sync(de_handle *h) {
   if (!h) return DE_ERR_INVALID;
   DE_CUDA(h, cudaSetDevice(h->device));
   DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_device_error(h);
+}
+
+int de_profile_epoch(de_handle *h, int32_t first_epoch, int32_t batch_size, int32_t ns, double lr,
+                     float *launch_ms, int32_t *launch_kind, int32_t capacity, int32_t *count) {
+  if (!h || !count) return DE_ERR_INVALID;
+  if (first_epoch < 0 || batch_size <= 0 || ns < 0) return fail(h, DE_ERR_INVALID, "bad epoch, batch_size or ns");
+  int rc = prepare_run(h, first_epoch, 1, batch_size, ns, &lr);
+  if (rc) return rc;
+  const std::vector<int> kinds = epoch_launch_kinds(h);
+  const int n = int(kinds.size());
+  *count = n;
+  if (!launch_ms || !launch_kind || capacity < n) return fail(h, DE_ERR_INVALID, "capacity below the launch count");
+  std::vector<cudaEvent_t> ev(n + 1, nullptr);
+  for (auto &e : ev) DE_CUDA(h, cudaEventCreate(&e));
+  cudaError_t err = enqueue_epoch(h, ns, h->stream, ev.data());
+  if (err == cudaSuccess) err = cudaEventRecord(ev[n], h->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
+  for (int i = 0; err == cudaSuccess && i < n; ++i) {
+    err = cudaEventElapsedTime(&launch_ms[i], ev[i], ev[i + 1]);
+    launch_kind[i] = kinds[i];
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (err != cudaSuccess) return cuda_fail(h, err, "profiled epoch");
   return check_device_error(h);
 }
 

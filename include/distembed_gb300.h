@@ -98,6 +98,17 @@ int de_run(de_handle *h, int32_t epochs, int32_t batch_size, int32_t ns,
 int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch_size, int32_t ns,
                 const double *lr_per_epoch, double *loss_per_epoch);
 
+/* Runs one epoch (epoch first_epoch of a call, one learning rate) like de_run_from,
+ * but launches its kernels one by one with CUDA events between them and waits:
+ * launch_ms[i] is the device time of launch i and launch_kind[i] its kind (0: the
+ * minibatch kernel of the FP32 form / the attractive kernel of the BF16 form,
+ * 1: BF16 repulsion GEMM kernel, 2: BF16 exact-row kernel, 3: epoch flush).
+ * *count receives the number of launches; capacity must be at least that.  The
+ * epoch is a real step: the embedding is updated.  No reference counterpart:
+ * this is the per-kernel timing used by the benchmark. */
+int de_profile_epoch(de_handle *h, int32_t first_epoch, int32_t batch_size, int32_t ns, double lr,
+                     float *launch_ms, int32_t *launch_kind, int32_t capacity, int32_t *count);
+
 /* Waits for all queued work of the handle. */
 int de_sync(de_handle *h);
 
