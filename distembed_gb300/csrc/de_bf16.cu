@@ -14,8 +14,9 @@
 // The factorisation drops the per-component clip of algo.hpp:643, which is exact
 // when no component can reach the bound: |c (x_d - n_d)| <= c sqrt(r) < 5 for
 // r >= 0.25.  A pair with r < 0.25 (other than a row drawn as its own negative,
-// whose force is exactly zero) flags its row; flagged rows are recomputed pair by
-// pair in FP32 with the clip by bf16_fixup_kernel.
+// whose force is exactly zero) is left out of the GEMMs and recorded in a
+// per-row bitmask; bf16_fixup_kernel adds those pairs one by one in FP32 with the
+// clip, then updates the row.
 //
 // Per minibatch: bf16_attract_kernel (attractive pass, warp per work item, plus
 // CTAs that gather the negatives into N / N^T), bf16_repulse_kernel (GEMMs and the
@@ -36,6 +37,8 @@ constexpr float kNearR = 0.25f;   // below this squared distance a component may
 constexpr int kTileRows = 128;    // rows per tcgen05 tile (M)
 constexpr int kChunk = 64;        // negatives per GEMM chunk (one 128-B swizzle atom)
 constexpr long kSpinLimit = 1L << 22;
+constexpr int kMaxKpad = 1024;    // negatives per minibatch in the BF16 form (bitmask words: 32)
+constexpr int kNearWords = kMaxKpad / 32;
 
 // ------------------------------------------------------------ BF16 rows
 // Lane l holds components [l*N, l*N + N) of a row, N = dim / 32.
@@ -470,6 +473,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       // Loss terms: the log of a product of eight ratios (each (1+r)/(r+1e-6)
       // in [1, 5] for the pairs taken), summed in FP32, folded into FP64 once.
       uint32_t packed[16];
+      uint32_t near_word = 0;  // bit i: column hf*32 + i of this chunk takes the exact path
       float loss_c = 0.f;
 #pragma unroll
       for (int j = 0; j < 32; j += 8) {
@@ -489,7 +493,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
           cv[q] = use ? cc : 0.f;
           prod *= use ? (1.0f + r) * inv : 1.0f;
           self_loss += (rep_active && self) ? kSelfLoss : 0.f;
-          near |= nearp;
+          near_word |= nearp ? (1u << (j + q)) : 0u;
           rowsum += cv[q];
         }
 #pragma unroll
@@ -500,6 +504,10 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         loss_c += __logf(prod);
       }
       loss += double(loss_c);
+      if (near_word) {
+        near = true;
+        a.near_bits[size_t(row_local) * kNearWords + c * 2 + hf] = near_word;
+      }
       if (c >= 2) mbar_wait(B(C_FREE + b), ((c >> 1) + 1) & 1, &err);
       unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
@@ -525,11 +533,14 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     loss = loss_part[t] + loss_part[kTileRows + t];
     near = (near_part[t] | near_part[kTileRows + t]) != 0;
     if (hf == 0 && row_valid && near && done) {
-      // recomputed pair by pair, with the clip, by bf16_fixup_kernel
+      // the pairs of near_bits are added, with the clip, by bf16_fixup_kernel
       const int slot = atomicAdd(a.flag_count, 1);
       a.flag_rows[slot] = row_local;
     }
-    const bool update = row_valid && !near && done;
+    // rows with exact-path pairs: the GEMM part of the update goes to abuf and
+    // bf16_fixup_kernel applies it; every other row is updated here
+    const bool update = row_valid && done;
+    const bool defer = near;
     const int dlo = hf * (D / 2);
     float *xm = a.xm + size_t(row_global) * D + dlo;
     __nv_bfloat16 *xb = a.xb + size_t(row_global) * D + dlo;
@@ -555,14 +566,26 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
             const float2 xv = __bfloat1622float2(xh[q]);
             const float f0 = rowsum * xv.x - __uint_as_float(f[d + 2 * q]);
             const float f1 = rowsum * xv.y - __uint_as_float(f[d + 2 * q + 1]);
-            m[2 * q] += av[2 * q] + lr * f0;
-            m[2 * q + 1] += av[2 * q + 1] + lr * f1;
+            const float p0 = av[2 * q] + lr * f0, p1 = av[2 * q + 1] + lr * f1;
+            if (defer) {
+              m[2 * q] = p0;
+              m[2 * q + 1] = p1;
+            } else {
+              m[2 * q] += p0;
+              m[2 * q + 1] += p1;
+            }
             __nv_bfloat162 p = __floats2bfloat162_rn(m[2 * q], m[2 * q + 1]);
             outp[q] = *reinterpret_cast<uint32_t *>(&p);
           }
-          *reinterpret_cast<float4 *>(xm + d0 + d) = make_float4(m[0], m[1], m[2], m[3]);
-          *reinterpret_cast<float4 *>(xm + d0 + d + 4) = make_float4(m[4], m[5], m[6], m[7]);
-          *reinterpret_cast<uint4 *>(xb + d0 + d) = make_uint4(outp[0], outp[1], outp[2], outp[3]);
+          if (defer) {
+            float *abw = const_cast<float *>(ab) + d0 + d;
+            *reinterpret_cast<float4 *>(abw) = make_float4(m[0], m[1], m[2], m[3]);
+            *reinterpret_cast<float4 *>(abw + 4) = make_float4(m[4], m[5], m[6], m[7]);
+          } else {
+            *reinterpret_cast<float4 *>(xm + d0 + d) = make_float4(m[0], m[1], m[2], m[3]);
+            *reinterpret_cast<float4 *>(xm + d0 + d + 4) = make_float4(m[4], m[5], m[6], m[7]);
+            *reinterpret_cast<uint4 *>(xb + d0 + d) = make_uint4(outp[0], outp[1], outp[2], outp[3]);
+          }
         }
       }
     }
@@ -580,64 +603,61 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
 
 // ------------------------------------------------------------ exact rows
 
-// Flagged rows: the repulsive pass pair by pair in FP32 on the BF16 values, with
-// the per-component clip (algo.hpp:633-645), then the update.  One CTA per row,
-// warp w takes negatives w, w+8, ...; the warps' sums are added in warp order.
+// Rows with exact-path pairs: one warp per row adds those pairs in FP32 on the
+// BF16 values with the per-component clip (algo.hpp:633-645), in negative
+// order, to the GEMM part of the update left in abuf, then updates the row and
+// clears its bitmask.
 template <int D>
 __global__ void __launch_bounds__(256) bf16_fixup_kernel(const BF16BatchArgs a) {
-  __shared__ float part[8][D];
-  __shared__ double part_loss[8];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int count = *a.flag_count;
   const int epoch = a.epoch[0];
   const float lr = a.lr[epoch];
-  for (int s = blockIdx.x; s < count; s += gridDim.x) {
+  constexpr int N = D / 32;
+  for (int s = gw; s < count; s += gridDim.x * 8) {
     const int row_local = a.flag_rows[s];
     const int row = a.base + row_local;
+    uint32_t *bits_row = a.near_bits + size_t(row_local) * kNearWords;
+    const uint32_t my_word = lane < kNearWords ? bits_row[lane] : 0u;
     Frag<D> xi, acc;
     load_bf16_row(xi, a.xb + size_t(row) * D, lane);
     acc.zero();
     float loss = 0.f;
-    for (int k = w; k < a.kpad; k += 8) {
-      const int nid = __ldg(a.nid + k);
-      if (nid < 0) continue;
-      if (nid == row) {
-        if (lane == 0) loss += __logf(1.0f / 1e-6f);
-        continue;
+    for (int w = 0; w < kNearWords; ++w) {
+      uint32_t bits = __shfl_sync(kFull, my_word, w);
+      while (bits) {
+        const int i = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int k = (w >> 1) * kChunk + (w & 1) * 32 + i;  // word w = 2 * chunk + half
+        Frag<D> xn;
+        load_bf16_row(xn, a.nb + size_t(k) * D, lane);
+        float diff[N];
+        float p = 0.f;
+#pragma unroll
+        for (int t = 0; t < N; ++t) {
+          diff[t] = xi.v[t] - xn.v[t];
+          p = fmaf(diff[t], diff[t], p);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
+        const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
+#pragma unroll
+        for (int t = 0; t < N; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
+        loss += logf((1.0f + p) / (p + 1e-6f));
       }
-      Frag<D> xn;
-      load_bf16_row(xn, a.nb + size_t(k) * D, lane);
-      float diff[D / 32];
-      float p = 0.f;
-#pragma unroll
-      for (int t = 0; t < D / 32; ++t) {
-        diff[t] = xi.v[t] - xn.v[t];
-        p = fmaf(diff[t], diff[t], p);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
-      const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
-#pragma unroll
-      for (int t = 0; t < D / 32; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
-      if (lane == 0) loss += logf((1.0f + p) / (p + 1e-6f));
     }
+    if (lane < kNearWords) bits_row[lane] = 0u;
+    float *xm = a.xm + size_t(row) * D + lane * N;
+    __nv_bfloat16 *xb = a.xb + size_t(row) * D + lane * N;
+    const float *ab = a.abuf + size_t(row_local) * D + lane * N;
 #pragma unroll
-    for (int t = 0; t < D / 32; ++t) part[w][lane * (D / 32) + t] = acc.v[t];
-    if (lane == 0) part_loss[w] = double(loss);
-    __syncthreads();
-    for (int d = threadIdx.x; d < D; d += 256) {
-      float r = 0.f;
-      for (int q = 0; q < 8; ++q) r += part[q][d];
-      const float m = a.xm[size_t(row) * D + d] + a.abuf[size_t(row_local) * D + d] + r;
-      a.xm[size_t(row) * D + d] = m;
-      a.xb[size_t(row) * D + d] = __float2bfloat16(m);
+    for (int t = 0; t < N; ++t) {
+      const float m = xm[t] + ab[t] + acc.v[t];
+      xm[t] = m;
+      xb[t] = __float2bfloat16(m);
     }
-    if (threadIdx.x == 0) {
-      double l = 0.0;
-      for (int q = 0; q < 8; ++q) l += part_loss[q];
-      a.loss_row[row] = l;
-    }
-    __syncthreads();
+    if (lane == 0) a.loss_row[row] += double(loss);
   }
 }
 
@@ -713,7 +733,7 @@ cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
   const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps < 64 ? (a.kpad + kPlainWarps - 1) / kPlainWarps : 64;
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
-  const int fix_ctas = 16;
+  const int fix_ctas = 128;
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };

@@ -98,6 +98,8 @@ struct de_handle {
   int32_t *d_flag_rows = nullptr;
   size_t flag_cap = 0;
   int32_t *d_flag_count = nullptr;
+  uint32_t *d_near_bits = nullptr;  // [B, 32], zero between minibatches
+  size_t near_cap = 0;
   double *d_loss_row = nullptr;
   int32_t *d_err = nullptr;
   int kpad = 0;
@@ -285,6 +287,7 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.nid = h->d_nid;
     a.flag_rows = h->d_flag_rows;
     a.flag_count = h->d_flag_count;
+    a.near_bits = h->d_near_bits;
     a.loss_item = h->d_loss_partial;
     a.loss_off = s.item_off[j];
     a.loss_row = h->d_loss_row;
@@ -312,11 +315,17 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
 int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
   const Schedule &s = h->sched;
   const int kpad = std::max(64, (ns + 63) / 64 * 64);
-  bool m = false;
+  if (kpad > 1024) return fail(h, DE_ERR_UNSUPPORTED, "the BF16 form takes at most 1024 negatives per minibatch");
+  bool m = false, near_moved = false;
   int rc = DE_OK;
   if ((rc = grow(h, &h->d_abuf, &h->abuf_cap, size_t(s.batch) * h->dim, &m)) ||
-      (rc = grow(h, &h->d_flag_rows, &h->flag_cap, size_t(s.batch), &m)))
+      (rc = grow(h, &h->d_flag_rows, &h->flag_cap, size_t(s.batch), &m)) ||
+      (rc = grow(h, &h->d_near_bits, &h->near_cap, size_t(s.batch) * 32, &near_moved)))
     return rc;
+  if (near_moved) {
+    DE_CUDA(h, cudaMemset(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t)));
+    m = true;
+  }
   if (size_t(kpad) > h->kpad_cap || !h->d_nn) {
     for (void *p : {static_cast<void *>(h->d_nn), static_cast<void *>(h->d_nid), static_cast<void *>(h->d_nb),
                     static_cast<void *>(h->d_nbt)})
@@ -448,6 +457,7 @@ int check_device_error(de_handle *h) {
   DE_CUDA(h, cudaMemcpy(&e, h->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (e) {
     DE_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int32_t)));
+    if (h->d_near_bits) DE_CUDA(h, cudaMemset(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t)));
     return fail(h, DE_ERR_CUDA, "a device-side wait timed out; results of this call are not valid");
   }
   return DE_OK;
@@ -571,6 +581,7 @@ int de_destroy(de_handle *h) {
   cudaFree(h->d_nn);
   cudaFree(h->d_nid);
   cudaFree(h->d_flag_rows);
+  cudaFree(h->d_near_bits);
   cudaFree(h->d_loss_row);
   cudaFree(h->d_epoch);
   cudaFree(h->d_loss);

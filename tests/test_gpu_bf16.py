@@ -66,6 +66,23 @@ def test_one_minibatch_exact_row_path():
     assert rel_l2(x1 - x0, prev) <= ONE_STEP_REL
 
 
+@pytest.mark.parametrize("dim", [64, 256])
+def test_one_minibatch_mixed_near_and_far_pairs(dim):
+    # half the rows sit in a tight cluster (their mutual pairs clip and take the
+    # exact path), half are spread out (GEMM path): most rows have both kinds
+    n, rp, col = gg.knn_csr(900, 8, 6, 3, seed=45)
+    x0 = gg.init_embedding(n, dim, seed=6)
+    tight = np.arange(n) % 2 == 0
+    x0[tight] *= 0.008
+    x0 = bf16_round(x0)
+    prev, _ = oracle.batch_grad(rp, col, x0, n, 256, 0.02, 0, 0, n, quirks=True)
+    x1, _ = run_bf16(rp, col, x0, 1, n, 256, 0.02)
+    assert rel_l2(x1 - x0, prev) <= ONE_STEP_REL
+    # the same minibatch twice in a row: the bitmask of exact-path pairs starts clean
+    x2, _ = run_bf16(rp, col, x0, 1, n, 256, 0.02)
+    assert np.array_equal(x1, x2)
+
+
 def test_multi_epoch_loss_within_one_percent():
     n, rp, col = gg.rmat_csr(12, 8, seed=42)
     x0 = bf16_round(gg.init_embedding(n, 256, seed=3))
