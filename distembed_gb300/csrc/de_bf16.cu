@@ -456,9 +456,13 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     for (int c = 0; c < nchunks; ++c) {
       const int b = c & 1;
       if (c > 0) epi_sync();  // meta of chunk c visible; everyone is done with chunk c-1
-      if (c + 1 < nchunks && et < kChunk) {
-        const int kk = (c + 1) * kChunk + et;
-        negmeta[b ^ 1][et] = make_float2(__ldg(a.nn + kk), __int_as_float(__ldg(a.nid + kk)));
+      // next chunk's metadata: loads issued now, stored at the end of this chunk
+      const bool pre = c + 1 < nchunks && et < kChunk;
+      float pre_nn = 0.f;
+      int pre_id = -1;
+      if (pre) {
+        pre_nn = __ldg(a.nn + (c + 1) * kChunk + et);
+        pre_id = __ldg(a.nid + (c + 1) * kChunk + et);
       }
       uint32_t s_raw[32] = {};
       const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (c >> 1) & 1, &err));
@@ -516,6 +520,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
             make_uint4(packed[4 * j], packed[4 * j + 1], packed[4 * j + 2], packed[4 * j + 3]);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(B(C_FULL + b));
+      if (pre) negmeta[b ^ 1][et] = make_float2(pre_nn, __int_as_float(pre_id));
     }
     // every lane of a warp takes the same branch around the (warp-wide) TMEM loads
     const bool done = __all_sync(kFull, mbar_wait(B(F_DONE), 0, &err) && !failed());
