@@ -492,10 +492,12 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
           const float r = xx + m.x - 2.0f * __uint_as_float(s_raw[j + q]);
           const bool nearp = valid && r < kNearR;
           const bool use = valid && !nearp;
-          const float inv = __fdividef(1.0f, r + 1e-6f);
-          const float cc = __bfloat162float(__float2bfloat16(2.0f * inv * __fdividef(1.0f, 1.0f + r)));
+          // one reciprocal: q = 1/((r+1e-6)(1+r)), c = 2q, (1+r)/(r+1e-6) = (1+r)^2 q
+          const float r1 = 1.0f + r;
+          const float qr = __fdividef(1.0f, (r + 1e-6f) * r1);
+          const float cc = __bfloat162float(__float2bfloat16(2.0f * qr));
           cv[q] = use ? cc : 0.f;
-          prod *= use ? (1.0f + r) * inv : 1.0f;
+          prod *= use ? r1 * r1 * qr : 1.0f;
           self_loss += (rep_active && self) ? kSelfLoss : 0.f;
           near_word |= nearp ? (1u << (j + q)) : 0u;
           rowsum += cv[q];
@@ -542,59 +544,77 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       const int slot = atomicAdd(a.flag_count, 1);
       a.flag_rows[slot] = row_local;
     }
-    // rows with exact-path pairs: the GEMM part of the update goes to abuf and
-    // bf16_fixup_kernel applies it; every other row is updated here
-    const bool update = row_valid && done;
-    const bool defer = near;
-    const int dlo = hf * (D / 2);
-    float *xm = a.xm + size_t(row_global) * D + dlo;
-    __nv_bfloat16 *xb = a.xb + size_t(row_global) * D + dlo;
-    const float *ab = a.abuf + size_t(row_local) * D + dlo;
+    if (hf == 0 && row_valid && done) a.loss_row[row_global] = loss;
+    epi_sync();  // the staging below may overwrite the combine area
+
+    // Repulsive force rowsum * x - F of every tile row, staged as FP32 rows (pitch
+    // D + 4 floats) in the operand buffers, which no GEMM reads any more (at dim
+    // 256 it reaches into C[0]); x comes from the swizzled X tile.  Thread
+    // (row t, half hf) writes dims [hf D/2, (hf+1) D/2).
+    constexpr int kPitch = D + 4;
+    float *stage = reinterpret_cast<float *>(sm + L::offN);
+    static_assert(kTileRows * kPitch * 4 <= 2 * (L::kN + L::kT) + L::kC, "staging fits before C[1]");
     for (int d0 = 0; done && d0 < D / 2; d0 += 32) {
+      const int dg = hf * (D / 2) + d0;  // first dim of this group of 32
       uint32_t f[32];
-      tmem_ld32(tmem + lane_base + 256u + uint32_t(dlo + d0), f);
+      tmem_ld32(tmem + lane_base + 256u + uint32_t(dg), f);
       tmem_wait_ld();
-      if (update) {
+      const unsigned char *xrow = sm + L::offX + (dg >> 6) * (kTileRows * 128) + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
-        for (int d = 0; d < 32; d += 8) {
-          uint4 xu = *reinterpret_cast<const uint4 *>(xb + d0 + d);
-          const __nv_bfloat162 *xh = reinterpret_cast<const __nv_bfloat162 *>(&xu);
-          float4 m0 = *reinterpret_cast<const float4 *>(xm + d0 + d);
-          float4 m1 = *reinterpret_cast<const float4 *>(xm + d0 + d + 4);
-          float4 a0 = *reinterpret_cast<const float4 *>(ab + d0 + d);
-          float4 a1 = *reinterpret_cast<const float4 *>(ab + d0 + d + 4);
-          float m[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-          const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-          uint32_t outp[4];
+      for (int d = 0; d < 32; d += 8) {
+        const int chunk = ((dg & 63) + d) >> 3;  // 16-byte chunk within the 128-byte row
+        const uint4 xu = *reinterpret_cast<const uint4 *>(xrow + ((chunk ^ (t & 7)) << 4));
+        const __nv_bfloat162 *xh = reinterpret_cast<const __nv_bfloat162 *>(&xu);
+        float g[8];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 xv = __bfloat1622float2(xh[q]);
-            const float f0 = rowsum * xv.x - __uint_as_float(f[d + 2 * q]);
-            const float f1 = rowsum * xv.y - __uint_as_float(f[d + 2 * q + 1]);
-            const float p0 = av[2 * q] + lr * f0, p1 = av[2 * q + 1] + lr * f1;
-            if (defer) {
-              m[2 * q] = p0;
-              m[2 * q + 1] = p1;
-            } else {
-              m[2 * q] += p0;
-              m[2 * q + 1] += p1;
-            }
-            __nv_bfloat162 p = __floats2bfloat162_rn(m[2 * q], m[2 * q + 1]);
-            outp[q] = *reinterpret_cast<uint32_t *>(&p);
-          }
-          if (defer) {
-            float *abw = const_cast<float *>(ab) + d0 + d;
-            *reinterpret_cast<float4 *>(abw) = make_float4(m[0], m[1], m[2], m[3]);
-            *reinterpret_cast<float4 *>(abw + 4) = make_float4(m[4], m[5], m[6], m[7]);
-          } else {
-            *reinterpret_cast<float4 *>(xm + d0 + d) = make_float4(m[0], m[1], m[2], m[3]);
-            *reinterpret_cast<float4 *>(xm + d0 + d + 4) = make_float4(m[4], m[5], m[6], m[7]);
-            *reinterpret_cast<uint4 *>(xb + d0 + d) = make_uint4(outp[0], outp[1], outp[2], outp[3]);
-          }
+        for (int q = 0; q < 4; ++q) {
+          const float2 xv = __bfloat1622float2(xh[q]);
+          g[2 * q] = rowsum * xv.x - __uint_as_float(f[d + 2 * q]);
+          g[2 * q + 1] = rowsum * xv.y - __uint_as_float(f[d + 2 * q + 1]);
+        }
+        float *dst = stage + t * kPitch + dg + d;
+        *reinterpret_cast<float4 *>(dst) = make_float4(g[0], g[1], g[2], g[3]);
+        *reinterpret_cast<float4 *>(dst + 4) = make_float4(g[4], g[5], g[6], g[7]);
+      }
+    }
+    int *row_flags = reinterpret_cast<int *>(sC_ptr[1]);  // 1: update x, 2: defer to abuf
+    if (hf == 0) row_flags[t] = (row_valid && done) ? (near ? 2 : 1) : 0;
+    epi_sync();
+
+    // Coalesced update, one warp per row, each lane 8 consecutive dims:
+    // x += abuf + lr * force, or abuf += lr * force for rows finished by
+    // bf16_fixup_kernel.
+    constexpr int kPer = D / 32;
+    for (int rr = warp; rr < kTileRows; rr += kEpiThreads / 32) {
+      const int flag = row_flags[rr];
+      if (flag == 0) continue;
+      const int rl = tile_base + rr;
+      const size_t rg = size_t(a.base + rl);
+      const float *src = stage + rr * kPitch + lane * kPer;
+      float *abp = a.abuf + size_t(rl) * D + lane * kPer;
+      float *xmp = a.xm + rg * D + lane * kPer;
+      __nv_bfloat16 *xbp = a.xb + rg * D + lane * kPer;
+      float pv[kPer];
+#pragma unroll
+      for (int q = 0; q < kPer; q += 2) {
+        const float2 ab2 = *reinterpret_cast<const float2 *>(abp + q);
+        const float2 f2 = *reinterpret_cast<const float2 *>(src + q);
+        pv[q] = ab2.x + lr * f2.x;
+        pv[q + 1] = ab2.y + lr * f2.y;
+      }
+      if (flag == 2) {
+#pragma unroll
+        for (int q = 0; q < kPer; q += 2) *reinterpret_cast<float2 *>(abp + q) = make_float2(pv[q], pv[q + 1]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < kPer; q += 2) {
+          const float2 m2 = *reinterpret_cast<const float2 *>(xmp + q);
+          const float m0 = m2.x + pv[q], m1 = m2.y + pv[q + 1];
+          *reinterpret_cast<float2 *>(xmp + q) = make_float2(m0, m1);
+          *reinterpret_cast<__nv_bfloat162 *>(xbp + q) = __floats2bfloat162_rn(m0, m1);
         }
       }
     }
-    if (hf == 0 && update) a.loss_row[row_global] = loss;
   }
   tc_fence_before();
   __syncthreads();
