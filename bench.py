@@ -56,9 +56,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="max CSR entries per work item (0: automatic)")
-    p.add_argument("--form", default="plain", choices=["plain", "bf16"],
+    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched"],
                    help="plain: FP32 plain form on R-MAT s20 (default line); bf16: BF16 precision form vs the "
-                        "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives")
+                        "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives; batched: 512 graphs in one "
+                        "persistent launch, BF16 storage, vs the FP32 plain form on the same graphs")
+    p.add_argument("--graphs", type=int, default=512, help="batched form: number of graphs")
+    p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
     return p.parse_args()
 
 
@@ -384,12 +387,192 @@ def run_bf16_form(args):
     print(json.dumps(line), flush=True)
 
 
+W4 = dict(n_lo=500, n_hi=50000, seed=3, dim=64, batch=256, ns=5, lr=0.02, epochs=20, init_seed=1000,
+          knn_k=10, knn_dim=32, rmat_ef=8)
+
+
+def batched_workload(count, device):
+    from distembed_gb300 import graphgen as gg
+    graphs = gg.graph_suite(count, W4["n_lo"], W4["n_hi"], W4["seed"], knn_k=W4["knn_k"], knn_dim=W4["knn_dim"],
+                            rmat_ef=W4["rmat_ef"], device=device)
+    x0 = [gg.init_embedding(n, W4["dim"], seed=W4["init_seed"] + i).astype(np.float32)
+          for i, (_, n, _, _) in enumerate(graphs)]
+    return graphs, x0
+
+
+def batched_bytes_per_epoch(graphs, dim, B, ns, s=2):
+    """Algorithmic bytes of one epoch of every graph (no reuse credited): per CSR
+    entry its column id and the BF16 neighbour row; per vertex its rowptr entry,
+    its own BF16 row read, the FP32 master read and written and the BF16 copy
+    written; per minibatch the ns negative rows."""
+    tot = 0
+    for _, n, rp, c in graphs:
+        nnz_eff = len(c) - int(np.sum(c == n - 1))
+        batches = (n + B - 1) // B
+        tot += nnz_eff * (4 + dim * s) + n * (8 + dim * s + 2 * dim * 4 + dim * s) + batches * ns * dim * s
+    return tot
+
+
+def run_batched_form(args):
+    """Batched form: every graph of the suite trained for 20 epochs in one persistent
+    launch (BF16 storage, FP32 master), against the FP32 plain form on the same
+    graphs one after the other."""
+    import torch
+
+    import distembed_gb300 as de
+    import oracle
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    graphs, x0 = batched_workload(args.graphs, "cuda")
+    gen_s = time.perf_counter() - t0
+    dim, B, ns, lr, E = W4["dim"], W4["batch"], W4["ns"], W4["lr"], W4["epochs"]
+    total_n = int(sum(n for _, n, _, _ in graphs))
+    total_nnz = int(sum(len(c) for _, _, _, c in graphs))
+    x0_all = np.concatenate(x0)
+
+    b = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="bf16")
+    stream = torch.cuda.ExternalStream(b.stream, device=0)
+    b.set_embeddings(-1, x0_all)
+    t0 = time.perf_counter()
+    shape, tune_ms = b.autotune(1, B, ns, lr)
+    tune_s = time.perf_counter() - t0
+    upd = b.edge_updates(E, B, ns)
+    b.prepare(E, B, ns, lr)
+    # the job's own loss: one launch from the initial embedding
+    b.set_embeddings(-1, x0_all)
+    b.launch()
+    loss_bf16 = b.wait()
+    for _ in range(args.warmup):
+        b.launch()
+    b.wait()
+    clocks = Clocks(0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev[0].record(stream)
+    for k in range(args.steps):
+        b.launch()
+        ev[k + 1].record(stream)
+    b.wait()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_s = sum(step_ms) / 1e3
+    value = upd * args.steps / total_s
+
+    # end to end through the public API: pinned host FP32 in, the job, host out
+    x_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+    x_host[:] = x0_all
+    out_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+    e2e_t = []
+    for k in range(max(args.e2e_steps, 0) + 1):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        b.set_embeddings(-1, x_host)
+        b.launch()
+        b.wait()
+        b.get_embeddings(-1, out=out_host)
+        if k > 0:
+            e2e_t.append(time.perf_counter() - t1)
+    e2e = None
+    if e2e_t:
+        e2e_s = statistics.mean(e2e_t)
+        e2e = {"value": upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": total_n * dim * 4,
+               "d2h_bytes_per_step": total_n * dim * 4, "ms_per_step": 1e3 * e2e_s,
+               "step": "host FP32 embeddings of every graph in, the 20-epoch job, host FP32 out (pinned)"}
+    b.close()
+
+    # FP32 storage in the same batched launch: the loss the BF16 storage is held to
+    bf = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="fp32")
+    bf.set_shape(*shape)
+    bf.set_embeddings(-1, x0_all)
+    loss_fp32 = bf.run(E, B, ns, lr)
+    bf.close()
+    gap_fp32 = np.abs(loss_bf16[:, -1] - loss_fp32[:, -1]) / loss_fp32[:, -1]
+
+    # FP64 oracle on a sample of graphs (the 8 smallest), full job
+    order = np.argsort([n for _, n, _, _ in graphs])[:8]
+    gaps = []
+    for i in order:
+        _, n, rp, c = graphs[i]
+        _, lo = oracle.run(rp, c, x0[i].astype(np.float64), E, B, ns, lr, quirks=True, threads=os.cpu_count() or 1)
+        gaps.append(abs(loss_bf16[i, -1] - lo[-1]) / lo[-1])
+
+    # FP32 plain form on the same graphs, one graph after another
+    plain = None
+    if not args.no_plain_compare:
+        plain_ms, plain_upd = 0.0, 0
+        for i, (_, n, rp, c) in enumerate(graphs):
+            with de.Handle(rp, c, dim, quirks=True, compute_loss=True) as h:
+                st = torch.cuda.ExternalStream(h.stream, device=0)
+                h.set_embeddings(x0[i])
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                h.run(1, B, ns, lr, want_loss=False)            # capture outside the timed region
+                h.set_embeddings(x0[i])
+                h.sync()
+                e0.record(st)
+                h.run(E, B, ns, lr, want_loss=False)
+                e1.record(st)
+                h.sync()
+                plain_ms += e0.elapsed_time(e1)
+                plain_upd += h.edge_updates(E, B, ns)
+        plain = {"edge_updates_per_s": plain_upd / (plain_ms / 1e3), "job_ms": plain_ms,
+                 "note": "FP32 plain form, one graph after another, device time of each 20-epoch job summed"}
+
+    alg = batched_bytes_per_epoch(graphs, dim, B, ns) * E
+    mean_s = statistics.mean(step_ms) / 1e3
+    peak, peak_kind = measured_peak()
+    achieved = alg / mean_s / 1e9
+
+    # CPU baseline: the FP64 oracle, all host cores, whole jobs of graphs in suite order
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        done, t1 = 0, time.perf_counter()
+        for i, (_, n, rp, c) in enumerate(graphs):
+            oracle.run(rp, c, x0[i].astype(np.float64), 1, B, ns, lr, quirks=True, threads=threads)
+            done += 1
+            if time.perf_counter() - t1 >= args.cpu_seconds:
+                break
+        dt = time.perf_counter() - t1
+        with de.Batch([(rp, c) for _, _, rp, c in graphs[:done]], dim) as bc:
+            cu = bc.edge_updates(1, B, ns)
+        cpu = {"value": cu / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"epoch 0 of graphs 0..{done - 1} of the suite, FP64, {cu} edge-updates in {dt:.1f} s"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": f"synthetic: {len(graphs)} graphs, n log-uniform [500, 50000] (seed 3), even: kNN k=10 of 32-D "
+                    "10-component mixtures, odd: R-MAT ef 8; U[-0.5,0.5] init (seed 1000+i)",
+            "config": {"workload": f"batched{len(graphs)}_d64_b256_ns5_e20_bf16", "graphs": len(graphs),
+                       "vertices": total_n, "nnz": total_nnz, "dim": dim, "batch": B, "ns": ns, "lr": lr,
+                       "epochs_per_job": E, "step": "one launch: every graph, 20 epochs (CUDA graph)",
+                       "l2": f"inputs larger than L2 ({total_n * dim * 6 / 2**30:.2f} GiB of embeddings); no flush",
+                       "team_shape": {"vertices_per_warp": shape[0], "team_warps": shape[1], "edge_cap": shape[2]},
+                       "autotune_s": round(tune_s, 2), "autotune_shapes": len(tune_ms),
+                       "generate_s": round(gen_s, 1)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": None, "kernel": "batched_kernel",
+                         "algorithmic_bytes_per_launch": alg},
+            "loss": {"final_gap_vs_fp32_storage_max": float(gap_fp32.max()),
+                     "final_gap_vs_fp32_storage_mean": float(gap_fp32.mean()),
+                     "final_gap_vs_fp64_oracle_sample_max": float(max(gaps)), "oracle_sample_graphs": len(gaps)},
+            "compare": {"fp32_plain": plain,
+                        "batched_over_plain": (value / plain["edge_updates_per_s"]) if plain else None},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.form == "bf16":
         run_bf16_form(args)
+    elif args.form == "batched":
+        run_batched_form(args)
     else:
         run_ours(args)
 

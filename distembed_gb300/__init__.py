@@ -33,7 +33,10 @@ PRECISION = {"fp32": 0, "bf16": 1}
 EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings", "de_get_embeddings",
            "de_set_embeddings_f32", "de_get_embeddings_f32", "de_run", "de_run_from", "de_profile_epoch", "de_sync",
            "de_edge_updates",
-           "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version")
+           "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version",
+           "de_batch_create", "de_batch_destroy", "de_batch_set_embeddings_f32", "de_batch_get_embeddings_f32",
+           "de_batch_set_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
+           "de_batch_last_error")
 
 
 class DEError(RuntimeError):
@@ -83,6 +86,24 @@ def lib():
         L.de_last_error.argtypes = [_vp]
         L.de_last_error.restype = ctypes.c_char_p
         L.de_version.restype = ctypes.c_char_p
+        L.de_batch_create.argtypes = [_i32, _vp, _vp, _vp, _i32, ctypes.POINTER(Options), ctypes.POINTER(_vp)]
+        L.de_batch_destroy.argtypes = [_vp]
+        L.de_batch_set_embeddings_f32.argtypes = [_vp, _i32, _vp]
+        L.de_batch_get_embeddings_f32.argtypes = [_vp, _i32, _vp]
+        L.de_batch_set_shape.argtypes = [_vp, _i32, _i32, _i32]
+        L.de_batch_run.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp]
+        L.de_batch_prepare.argtypes = [_vp, _i32, _i32, _i32, _vp]
+        L.de_batch_launch.argtypes = [_vp]
+        L.de_batch_wait.argtypes = [_vp, _vp]
+        L.de_batch_autotune.argtypes = [_vp, _i32, _i32, _i32, ctypes.c_double, _vp, _i32, _vp, _vp, _vp, _vp]
+        L.de_batch_edge_updates.argtypes = [_vp, _i32, _i32, _i32]
+        L.de_batch_edge_updates.restype = _i64
+        L.de_batch_set_near_distance.argtypes = [_vp, ctypes.c_float]
+        L.de_batch_trace.argtypes = [_vp, _vp]
+        L.de_batch_stream.argtypes = [_vp]
+        L.de_batch_stream.restype = _vp
+        L.de_batch_last_error.argtypes = [_vp]
+        L.de_batch_last_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
 
@@ -237,3 +258,126 @@ class EmbeddingAlgo:
         self.last_loss = self.handle.run(iterations, batch_size, ns, lr, want_loss=True)
         self.handle.get_embeddings(out=self.dense)
         return self.last_loss
+
+
+class Batch:
+    """Many independent graphs trained in one persistent launch (de_batch_*).
+
+    graphs: a list of (rowptr, col) CSR pairs with local vertex ids.  Every graph
+    follows the reference's one-rank step on its own, with its own sampler seeds,
+    so its result does not depend on the other graphs of the batch."""
+
+    def __init__(self, graphs, dim: int, precision: str = "fp32", quirks: bool = True, device: int = 0,
+                 stream: int | None = None, max_bound: float = 5.0, edge_cap: int = 0):
+        L = lib()
+        self._rp = [np.ascontiguousarray(rp, dtype=np.int64) for rp, _ in graphs]
+        self._col = [np.ascontiguousarray(c, dtype=np.int64) if len(c) else np.zeros(1, np.int64)
+                     for _, c in graphs]
+        self.n = np.array([len(rp) - 1 for rp in self._rp], dtype=np.int64)
+        self.dim = dim
+        o = Options()
+        L.de_default_options(ctypes.byref(o))
+        o.precision = PRECISION[precision]
+        o.ref_quirks = int(quirks)
+        o.device = device
+        o.stream = stream
+        o.max_bound = max_bound
+        o.edge_cap = edge_cap
+        rps = (ctypes.c_void_p * len(graphs))(*[a.ctypes.data for a in self._rp])
+        cols = (ctypes.c_void_p * len(graphs))(*[a.ctypes.data for a in self._col])
+        h = _vp()
+        rc = L.de_batch_create(len(graphs), self.n.ctypes.data, rps, cols, dim, ctypes.byref(o), ctypes.byref(h))
+        if rc != DE_OK:
+            raise DEError(rc, L.de_batch_last_error(None).decode())
+        self._h = h
+
+    def _check(self, rc: int):
+        if rc != DE_OK:
+            raise DEError(rc, lib().de_batch_last_error(self._h).decode())
+
+    @property
+    def stream(self) -> int:
+        return lib().de_batch_stream(self._h)
+
+    def _rows(self, g: int) -> int:
+        return int(self.n.sum()) if g < 0 else int(self.n[g])
+
+    def set_embeddings(self, g: int, x):
+        """Graph g's FP32 (n[g], dim) embedding; g = -1: all graphs concatenated."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        assert x.shape == (self._rows(g), self.dim)
+        self._check(lib().de_batch_set_embeddings_f32(self._h, g, x.ctypes.data))
+
+    def get_embeddings(self, g: int, out=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self._rows(g), self.dim), dtype=np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == (self._rows(g), self.dim)
+        self._check(lib().de_batch_get_embeddings_f32(self._h, g, out.ctypes.data))
+        return out
+
+    def set_shape(self, vertices_per_warp: int, team_warps: int, edge_cap: int):
+        self._check(lib().de_batch_set_shape(self._h, vertices_per_warp, team_warps, edge_cap))
+
+    def run(self, epochs: int, batch_size: int, ns: int, lr) -> np.ndarray:
+        """Trains every graph; returns the FP64 loss, shape (graphs, epochs)."""
+        lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+        loss = np.zeros((len(self.n), max(epochs, 1)), dtype=np.float64)
+        self._check(lib().de_batch_run(self._h, epochs, batch_size, ns, lrs.ctypes.data, loss.ctypes.data))
+        return loss[:, :epochs]
+
+    def prepare(self, epochs: int, batch_size: int, ns: int, lr):
+        """Host preparation and CUDA-graph capture of one run (nothing runs)."""
+        self._epochs = epochs
+        lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+        self._check(lib().de_batch_prepare(self._h, epochs, batch_size, ns, lrs.ctypes.data))
+
+    def launch(self):
+        """Replays the prepared run on the batch's stream; returns at once."""
+        self._check(lib().de_batch_launch(self._h))
+
+    def wait(self) -> np.ndarray:
+        """Waits; returns the (graphs, epochs) FP64 loss of the last launch."""
+        loss = np.zeros((len(self.n), max(self._epochs, 1)), dtype=np.float64)
+        self._check(lib().de_batch_wait(self._h, loss.ctypes.data))
+        return loss[:, :self._epochs]
+
+    def autotune(self, epochs: int, batch_size: int, ns: int, lr: float):
+        """Times every team shape on `epochs` real epochs (embeddings restored) and
+        keeps the fastest.  Returns ((vpw, warps, edge_cap), ms of each shape tried)."""
+        cap = 64
+        ms = np.zeros(cap, dtype=np.float32)
+        cnt = ctypes.c_int32(0)
+        v, w, c = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+        self._check(lib().de_batch_autotune(self._h, epochs, batch_size, ns, lr, ms.ctypes.data, cap,
+                                            ctypes.byref(cnt), ctypes.byref(v), ctypes.byref(w), ctypes.byref(c)))
+        return (v.value, w.value, c.value), ms[:cnt.value]
+
+    def edge_updates(self, epochs: int, batch_size: int, ns: int) -> int:
+        return int(lib().de_batch_edge_updates(self._h, epochs, batch_size, ns))
+
+    def set_near_distance(self, near_r: float):
+        self._check(lib().de_batch_set_near_distance(self._h, near_r))
+
+    def trace(self) -> np.ndarray:
+        """(graphs, 3): start and end (ns, from the earliest start) and team of each graph."""
+        out = np.zeros((len(self.n), 3), dtype=np.int64)
+        self._check(lib().de_batch_trace(self._h, out.ctypes.data))
+        out[:, :2] -= out[:, 0].min()
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().de_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -77,6 +77,17 @@ def rmat_csr(scale: int, edge_factor: int, seed: int, a=0.57, b=0.19, c=0.19):
     return n, *coo_to_csr(n, s, d)
 
 
+def rmat_csr_n(n: int, edge_factor: int, seed: int, a=0.57, b=0.19, c=0.19):
+    """R-MAT on n vertices (n need not be a power of two): edge_factor * 2**scale
+    edges are drawn at scale = ceil(log2 n) and those with an endpoint >= n are
+    dropped."""
+    scale = max(1, int(np.ceil(np.log2(max(n, 2)))))
+    s, d = rmat_edges(scale, edge_factor, a, b, c, seed)
+    keep = (s < n) & (d < n)
+    s, d = symmetrise(s[keep], d[keep])
+    return n, *coo_to_csr(n, s, d)
+
+
 # ------------------------------------------------------- Gaussian-mixture kNN
 
 def gaussian_mixture(n: int, dim: int, components: int, seed: int, mean_std: float = 2.0):
@@ -108,11 +119,49 @@ def knn_edges(pts: np.ndarray, k: int, block: int = 2048):
     return src, dst
 
 
-def knn_csr(n: int, dim: int, k: int, components: int, seed: int):
+def knn_edges_torch(pts: np.ndarray, k: int, device, block: int = 4096):
+    """k nearest neighbours on a torch device in FP32 (input preparation for large
+    suites; the FP64 knn_edges is the exact reference).  Self excluded."""
+    import torch
+    x = torch.as_tensor(np.asarray(pts, dtype=np.float32), device=device)
+    n = x.shape[0]
+    k = min(k, n - 1)
+    sq = (x * x).sum(1)
+    dst = torch.empty(n * k, dtype=torch.int64, device=device)
+    for lo in range(0, n, block):
+        hi = min(n, lo + block)
+        d2 = sq[lo:hi, None] + sq[None, :] - 2.0 * (x[lo:hi] @ x.T)
+        d2[torch.arange(hi - lo, device=device), torch.arange(lo, hi, device=device)] = float("inf")
+        dst[lo * k: hi * k] = torch.topk(d2, k, dim=1, largest=False).indices.reshape(-1)
+    src = np.repeat(np.arange(n, dtype=np.int64), k)
+    return src, dst.cpu().numpy()
+
+
+def knn_csr(n: int, dim: int, k: int, components: int, seed: int, device=None):
+    """Symmetrised kNN graph of a Gaussian mixture; device: compute the neighbours
+    with torch on that device (FP32) instead of numpy (FP64)."""
     pts, _ = gaussian_mixture(n, dim, components, seed)
-    s, d = knn_edges(pts, k)
+    s, d = knn_edges(pts, k) if device is None else knn_edges_torch(pts, k, device)
     s, d = symmetrise(s, d)
     return n, *coo_to_csr(n, s, d)
+
+
+def graph_suite(count: int, n_lo: int, n_hi: int, seed: int, knn_k: int = 10, knn_dim: int = 32,
+                knn_components: int = 10, rmat_ef: int = 8, device=None):
+    """`count` independent graphs, vertex counts log-uniform in [n_lo, n_hi]
+    (PCG64(seed)); even positions are kNN graphs (knn_k neighbours of knn_dim-D
+    mixtures), odd positions R-MAT graphs (edge factor rmat_ef).  Graph i is
+    seeded with seed * 100003 + i.  Returns a list of (kind, n, rowptr, col)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = np.rint(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), size=count))).astype(np.int64)
+    out = []
+    for i, n in enumerate(ns):
+        gs = seed * 100003 + i
+        if i % 2 == 0:
+            out.append(("knn", *knn_csr(int(n), knn_dim, knn_k, knn_components, gs, device=device)))
+        else:
+            out.append(("rmat", *rmat_csr_n(int(n), rmat_ef, gs)))
+    return out
 
 
 # ------------------------------------------------------------ embeddings

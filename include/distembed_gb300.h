@@ -142,6 +142,67 @@ int de_minibatch_noalloc(int64_t n, const int32_t *rowptr, const int32_t *col, i
                          int32_t rep_rows, int32_t skip_last_vertex, float lr, float max_bound,
                          double *loss, void *stream);
 
+/* ---- Batched form: many independent graphs trained in one persistent launch.
+ * No counterpart in the reference, which trains one graph per process
+ * (cpp/dist_embed.cpp:334-344 builds one EmbeddingAlgo and calls
+ * algo_force2_vec_ns once); each graph here follows that same one-rank step
+ * (cpp/algo/algo.hpp:164-192) with its own sampler seeds (epoch + batch), as if
+ * it ran alone.  One CTA ("team") owns a graph for all its epochs; teams take
+ * graphs largest first.  dim is 32, 64 or 128; opts->precision picks FP32
+ * storage or BF16 storage with an FP32 master copy; opts->edge_cap (0: 32) is the
+ * CSR entries of one work item, up to 4096. */
+typedef struct de_batch de_batch;
+
+/* Graph g has n[g] vertices and CSR rowptr[g][n[g]+1], col[g][rowptr[g][n[g]]]
+ * (local vertex ids).  Embeddings start at zero: set them before running. */
+int de_batch_create(int32_t n_graphs, const int64_t *n, const int64_t *const *rowptr,
+                    const int64_t *const *col, int32_t dim, const de_options *opts, de_batch **out);
+int de_batch_destroy(de_batch *b);
+/* Host FP32 (n[g] x dim) embedding of graph g in / out; graph = -1: every graph's,
+ * concatenated in graph order (sum of n x dim). */
+int de_batch_set_embeddings_f32(de_batch *b, int32_t graph, const float *x);
+int de_batch_get_embeddings_f32(de_batch *b, int32_t graph, float *x);
+/* Team shape: vertices per warp (1, 2 or 4: a work item on 32, 16 or 8 lanes),
+ * warps per team (4, 8, 16 or 32) and edge cap (1..4096). */
+int de_batch_set_shape(de_batch *b, int32_t vertices_per_warp, int32_t team_warps, int32_t edge_cap);
+/* Trains every graph for `epochs` epochs (minibatch batch_size, ns shared
+ * negatives per minibatch, lr_per_epoch[epochs]) in one launch captured in a CUDA
+ * graph, and waits.  loss (nullable): [n_graphs x epochs] FP64 per-graph epoch
+ * loss. */
+int de_batch_run(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, const double *lr_per_epoch,
+                 double *loss);
+/* de_batch_run in three parts.  prepare: builds the work lists, draws the
+ * negatives, allocates the team staging areas and captures the one launch in a
+ * CUDA graph (host work; nothing runs).  launch: replays that graph on the batch's
+ * stream and returns; every launch trains every graph for the prepared epochs
+ * again, from the embeddings it finds.  wait: waits for the stream and, when
+ * loss is given, copies the [n_graphs x epochs] loss of the last launch. */
+int de_batch_prepare(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, const double *lr_per_epoch);
+int de_batch_launch(de_batch *b);
+int de_batch_wait(de_batch *b, double *loss);
+/* Times every team shape (vertices per warp x team warps x edge caps 32..256) on
+ * `epochs` epochs of the real workload, keeps the fastest with de_batch_set_shape
+ * and leaves the embeddings as they were.  ms (nullable, capacity entries):
+ * the time of each shape tried, in the order vpw-major, then warps, then cap;
+ * *count (nullable) receives the number tried. */
+int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, double lr, float *ms,
+                      int32_t capacity, int32_t *count, int32_t *best_vpw, int32_t *best_warps,
+                      int32_t *best_edge_cap);
+/* BF16 form: a pair whose squared distance computed from the BF16 copies is below
+ * near_r (default 0.05) is read again from the FP32 master and recomputed; 0 turns
+ * this off.  Close pairs are the ones whose distance the BF16 rounding step
+ * distorts. */
+int de_batch_set_near_distance(de_batch *b, float near_r);
+/* Per graph of the last launch: {start, end} (globaltimer ns) and the team that
+ * ran it; out holds n_graphs x 3 values.  Waits for the stream. */
+int de_batch_trace(de_batch *b, int64_t *out);
+/* Edge-updates de_batch_run performs with these arguments, summed over graphs. */
+int64_t de_batch_edge_updates(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns);
+/* The cudaStream_t the batch runs on (as void*). */
+void *de_batch_stream(de_batch *b);
+/* Text of the last error on b (NULL: of the last failed de_batch_create). */
+const char *de_batch_last_error(const de_batch *b);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 

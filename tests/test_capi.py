@@ -75,3 +75,24 @@ def test_create_rejects_bad_input_before_touching_the_gpu(L, bad):
     with pytest.raises(de.DEError) as ei:
         de.Handle(rowptr, col, dim)
     assert ei.value.code == de.DE_ERR_INVALID
+
+
+@pytest.mark.parametrize("bad", ["rowptr_start", "decreasing", "col_range", "dim", "empty_graph"])
+def test_batch_create_rejects_bad_input_before_touching_the_gpu(L, bad):
+    rowptr = np.array([0, 2, 3, 4], dtype=np.int64)
+    col = np.array([1, 2, 0, 1], dtype=np.int64)
+    good = (np.array([0, 1, 2], dtype=np.int64), np.array([1, 0], dtype=np.int64))
+    dim = 64
+    if bad == "rowptr_start":
+        rowptr[0] = 1
+    elif bad == "decreasing":
+        rowptr[1:3] = [3, 2]
+    elif bad == "col_range":
+        col[2] = 3
+    elif bad == "dim":
+        dim = 256
+    else:
+        rowptr = np.array([0], dtype=np.int64)
+    with pytest.raises(de.DEError) as ei:
+        de.Batch([good, (rowptr, col)], dim)
+    assert ei.value.code == de.DE_ERR_INVALID

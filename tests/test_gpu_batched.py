@@ -1,0 +1,185 @@
+"""Batched form (many graphs in one persistent launch) against the FP64 oracle,
+through the C ABI.
+
+Each graph of a batch must train exactly as if it ran alone through the
+reference's one-rank step (its own sampler seeds, its own minibatch order).
+
+Tolerances:
+  FP32 storage   ||x_gpu - x_oracle||_2 / ||x_oracle||_2 <= 1e-4 per graph after
+                 several epochs; per-epoch loss within 1e-3 (relative)
+  BF16 storage   per-epoch loss within 1% of the FP64 oracle's (FP32 master and
+                 accumulation, every read BF16)
+  alone vs mix   bitwise equal, for one team shape: a graph's arithmetic does not
+                 depend on which team runs it or what else is in the batch
+"""
+import numpy as np
+import pytest
+
+import distembed_gb300 as de
+import oracle
+from distembed_gb300 import graphgen as gg
+
+pytestmark = pytest.mark.gpu
+
+RUN_REL_L2 = 1e-4
+LOSS_RTOL = 1e-3
+BF16_LOSS_GAP = 1e-2
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from distembed_gb300 import build
+    build.build()
+
+
+def f32(x):
+    return np.asarray(x, dtype=np.float32).astype(np.float64)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def suite():
+    """Small graphs of both kinds: sizes below, at and above the minibatch, a
+    partial last minibatch, hub rows longer than every edge cap tried."""
+    gs = [(k, n, rp, c) for k, n, rp, c in gg.graph_suite(6, 150, 2500, seed=11)]
+    n, rp, c = gg.rmat_csr_n(97, 8, seed=5)        # smaller than one minibatch
+    gs.append(("rmat", n, rp, c))
+    n, rp, c = gg.rmat_csr(10, 16, seed=6)         # hubs of several hundred entries
+    gs.append(("rmat", n, rp, c))
+    return gs
+
+
+GRAPHS = suite()
+
+
+def x_init(i, n, dim):
+    return f32(gg.init_embedding(n, dim, seed=100 + i))
+
+
+def run_batch(graphs, dim, epochs, batch, ns, lr, precision="fp32", shape=None, ids=None):
+    ids = list(range(len(graphs))) if ids is None else ids
+    with de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision=precision) as b:
+        if shape:
+            b.set_shape(*shape)
+        for j, (i, (_, n, _, _)) in enumerate(zip(ids, graphs)):
+            b.set_embeddings(j, x_init(i, n, dim))
+        loss = b.run(epochs, batch, ns, lr)
+        return [b.get_embeddings(j).astype(np.float64) for j in range(len(graphs))], loss
+
+
+@pytest.mark.parametrize("dim", [32, 64, 128])
+def test_fp32_batch_matches_oracle_per_graph(dim):
+    E, B, ns = 3, 256, 5
+    lr = [0.02 * (1 - e / E) for e in range(E)]
+    xs, loss = run_batch(GRAPHS, dim, E, B, ns, lr)
+    for i, (kind, n, rp, c) in enumerate(GRAPHS):
+        xo, lo = oracle.run(rp, c, x_init(i, n, dim), E, B, ns, lr, quirks=True)
+        assert rel_l2(xs[i], xo) <= RUN_REL_L2, (i, kind, n)
+        assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (i, loss[i], lo)
+
+
+@pytest.mark.parametrize("shape", [(1, 4, 32), (2, 8, 8), (4, 16, 64), (4, 8, 4096), (2, 32, 128)])
+def test_every_team_shape_matches_oracle(shape):
+    dim, E, B, ns = 64, 2, 128, 7
+    xs, loss = run_batch(GRAPHS, dim, E, B, ns, 0.03, shape=shape)
+    for i, (kind, n, rp, c) in enumerate(GRAPHS):
+        xo, lo = oracle.run(rp, c, x_init(i, n, dim), E, B, ns, 0.03, quirks=True)
+        assert rel_l2(xs[i], xo) <= RUN_REL_L2, (shape, i, kind, n)
+        assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (shape, i)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_alone_equals_mix_bitwise(precision):
+    dim, E, B, ns, shape = 64, 3, 256, 5, (4, 8, 32)
+    xs, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision=precision, shape=shape)
+    for i in (0, 3, len(GRAPHS) - 1):
+        xa, la = run_batch([GRAPHS[i]], dim, E, B, ns, 0.02, precision=precision, shape=shape, ids=[i])
+        assert np.array_equal(xa[0], xs[i]), i
+        assert np.array_equal(la[0], loss[i]), i
+    # the mix in another order gives the same per-graph results
+    perm = [5, 2, 7, 0, 6, 1, 4, 3]
+    xp, lp = run_batch([GRAPHS[i] for i in perm], dim, E, B, ns, 0.02, precision=precision, shape=shape,
+                       ids=perm)
+    for j, i in enumerate(perm):
+        assert np.array_equal(xp[j], xs[i]) and np.array_equal(lp[j], loss[i]), i
+
+
+def test_bf16_batch_loss_within_one_percent():
+    dim, E, B, ns = 64, 4, 256, 5
+    _, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16")
+    for i, (kind, n, rp, c) in enumerate(GRAPHS):
+        x0 = x_init(i, n, dim)
+        # the BF16 form starts from the BF16 rounding of the FP32 embedding
+        u = np.asarray(x0, dtype=np.float32).view(np.uint32).astype(np.uint64)
+        x0b = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32).view(np.float32)
+        _, lo = oracle.run(rp, c, x0b.astype(np.float64), E, B, ns, 0.02, quirks=True)
+        gap = np.abs(loss[i] - lo) / lo
+        assert np.all(gap <= BF16_LOSS_GAP), (i, kind, loss[i], lo)
+
+
+def test_autotune_keeps_embeddings_and_picks_a_valid_shape():
+    dim, B, ns = 64, 256, 5
+    graphs = GRAPHS[:4]
+    with de.Batch([(rp, c) for _, _, rp, c in graphs], dim) as b:
+        for i, (_, n, _, _) in enumerate(graphs):
+            b.set_embeddings(i, x_init(i, n, dim))
+        (v, w, c), ms = b.autotune(1, B, ns, 0.02)
+        assert v in (1, 2, 4) and w in (4, 8, 16, 32) and c in (32, 64, 128, 256)
+        assert len(ms) == 3 * 4 * 4 and np.all(ms > 0)
+        for i, (_, n, _, _) in enumerate(graphs):
+            assert np.array_equal(b.get_embeddings(i).astype(np.float64), x_init(i, n, dim))
+        loss = b.run(2, B, ns, 0.02)
+        got = [b.get_embeddings(i).astype(np.float64) for i in range(len(graphs))]
+    xs, ls = run_batch(graphs, dim, 2, B, ns, 0.02, shape=(v, w, c))
+    for i in range(len(graphs)):
+        assert np.array_equal(got[i], xs[i]) and np.array_equal(loss[i], ls[i])
+
+
+def test_edge_updates_is_the_sum_over_graphs():
+    dim, E, B, ns = 32, 3, 256, 5
+    with de.Batch([(rp, c) for _, _, rp, c in GRAPHS], dim) as b:
+        total = b.edge_updates(E, B, ns)
+    want = 0
+    for _, n, rp, c in GRAPHS:
+        with de.Handle(rp, c, dim) as h:
+            want += h.edge_updates(E, B, ns)
+    assert total == want
+
+
+def test_run_twice_continues_from_the_first():
+    # two calls of one epoch each = the oracle's two separate one-epoch calls
+    dim, B, ns = 64, 256, 5
+    graphs = GRAPHS[:3]
+    with de.Batch([(rp, c) for _, _, rp, c in graphs], dim) as b:
+        for i, (_, n, _, _) in enumerate(graphs):
+            b.set_embeddings(i, x_init(i, n, dim))
+        b.run(1, B, ns, 0.02)
+        b.run(1, B, ns, 0.02)
+        got = [b.get_embeddings(i).astype(np.float64) for i in range(len(graphs))]
+    for i, (_, n, rp, c) in enumerate(graphs):
+        x1, _ = oracle.run(rp, c, x_init(i, n, dim), 1, B, ns, 0.02, quirks=True)
+        x2, _ = oracle.run(rp, c, x1, 1, B, ns, 0.02, quirks=True)
+        assert rel_l2(got[i], x2) <= RUN_REL_L2
+
+
+def test_prepared_launch_replays_the_same_run():
+    dim, B, ns = 64, 256, 5
+    graphs = GRAPHS[:3]
+    with de.Batch([(rp, c) for _, _, rp, c in graphs], dim) as b:
+        for i, (_, n, _, _) in enumerate(graphs):
+            b.set_embeddings(i, x_init(i, n, dim))
+        b.prepare(1, B, ns, 0.02)
+        b.launch()
+        b.launch()
+        b.wait()
+        got = [b.get_embeddings(i).astype(np.float64) for i in range(len(graphs))]
+        b.run(1, B, ns, 0.02)
+        again = [b.get_embeddings(i).astype(np.float64) for i in range(len(graphs))]
+    for i, (_, n, rp, c) in enumerate(graphs):
+        x1, _ = oracle.run(rp, c, x_init(i, n, dim), 1, B, ns, 0.02, quirks=True)
+        x2, _ = oracle.run(rp, c, x1, 1, B, ns, 0.02, quirks=True)
+        x3, _ = oracle.run(rp, c, x2, 1, B, ns, 0.02, quirks=True)
+        assert rel_l2(got[i], x2) <= RUN_REL_L2
+        assert rel_l2(again[i], x3) <= RUN_REL_L2
