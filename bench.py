@@ -434,7 +434,7 @@ def run_batched_form(args):
     stream = torch.cuda.ExternalStream(b.stream, device=0)
     b.set_embeddings(-1, x0_all)
     t0 = time.perf_counter()
-    shape, tune_ms = b.autotune(1, B, ns, lr)
+    shape, tuned = b.autotune(1, B, ns, lr)
     tune_s = time.perf_counter() - t0
     upd = b.edge_updates(E, B, ns)
     b.prepare(E, B, ns, lr)
@@ -485,7 +485,7 @@ def run_batched_form(args):
 
     # FP32 storage in the same batched launch: the loss the BF16 storage is held to
     bf = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="fp32")
-    bf.set_shape(*shape)
+    bf.set_shape(**shape)
     bf.set_embeddings(-1, x0_all)
     loss_fp32 = bf.run(E, B, ns, lr)
     bf.close()
@@ -550,8 +550,8 @@ def run_batched_form(args):
                        "vertices": total_n, "nnz": total_nnz, "dim": dim, "batch": B, "ns": ns, "lr": lr,
                        "epochs_per_job": E, "step": "one launch: every graph, 20 epochs (CUDA graph)",
                        "l2": f"inputs larger than L2 ({total_n * dim * 6 / 2**30:.2f} GiB of embeddings); no flush",
-                       "team_shape": {"vertices_per_warp": shape[0], "team_warps": shape[1], "edge_cap": shape[2]},
-                       "autotune_s": round(tune_s, 2), "autotune_shapes": len(tune_ms),
+                       "team_shape": shape, "autotune_s": round(tune_s, 2), "autotune_shapes": len(tuned),
+                       "autotune_top5_ms": [[sh, round(t, 2)] for sh, t in sorted(tuned, key=lambda x: x[1])[:5]],
                        "generate_s": round(gen_s, 1)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": None, "kernel": "batched_kernel",

@@ -35,8 +35,19 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_edge_updates",
            "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version",
            "de_batch_create", "de_batch_destroy", "de_batch_set_embeddings_f32", "de_batch_get_embeddings_f32",
-           "de_batch_set_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
+           "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
            "de_batch_last_error")
+
+
+class BatchShape(ctypes.Structure):
+    _fields_ = [("kernel", ctypes.c_int32), ("vertices_per_warp", ctypes.c_int32), ("team_warps", ctypes.c_int32),
+                ("edge_cap", ctypes.c_int32), ("pairs", ctypes.c_int32), ("stages", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+BATCH_KERNEL = {"register": 0, "staged": 1}
 
 
 class DEError(RuntimeError):
@@ -90,12 +101,14 @@ def lib():
         L.de_batch_destroy.argtypes = [_vp]
         L.de_batch_set_embeddings_f32.argtypes = [_vp, _i32, _vp]
         L.de_batch_get_embeddings_f32.argtypes = [_vp, _i32, _vp]
-        L.de_batch_set_shape.argtypes = [_vp, _i32, _i32, _i32]
+        L.de_batch_set_shape.argtypes = [_vp, ctypes.POINTER(BatchShape)]
+        L.de_batch_get_shape.argtypes = [_vp, ctypes.POINTER(BatchShape)]
         L.de_batch_run.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp]
         L.de_batch_prepare.argtypes = [_vp, _i32, _i32, _i32, _vp]
         L.de_batch_launch.argtypes = [_vp]
         L.de_batch_wait.argtypes = [_vp, _vp]
-        L.de_batch_autotune.argtypes = [_vp, _i32, _i32, _i32, ctypes.c_double, _vp, _i32, _vp, _vp, _vp, _vp]
+        L.de_batch_autotune.argtypes = [_vp, _i32, _i32, _i32, ctypes.c_double, _vp, _vp, _i32, _vp,
+                                        ctypes.POINTER(BatchShape)]
         L.de_batch_edge_updates.argtypes = [_vp, _i32, _i32, _i32]
         L.de_batch_edge_updates.restype = _i64
         L.de_batch_set_near_distance.argtypes = [_vp, ctypes.c_float]
@@ -315,8 +328,16 @@ class Batch:
         self._check(lib().de_batch_get_embeddings_f32(self._h, g, out.ctypes.data))
         return out
 
-    def set_shape(self, vertices_per_warp: int, team_warps: int, edge_cap: int):
-        self._check(lib().de_batch_set_shape(self._h, vertices_per_warp, team_warps, edge_cap))
+    def set_shape(self, kernel="register", vertices_per_warp=0, team_warps=8, edge_cap=32, pairs=0, stages=0):
+        """Team shape (see de_batch_shape); kernel "register" or "staged" (or 0 / 1)."""
+        k = BATCH_KERNEL.get(kernel, kernel)
+        sh = BatchShape(k, vertices_per_warp, team_warps, edge_cap, pairs, stages)
+        self._check(lib().de_batch_set_shape(self._h, ctypes.byref(sh)))
+
+    def shape(self) -> dict:
+        sh = BatchShape()
+        self._check(lib().de_batch_get_shape(self._h, ctypes.byref(sh)))
+        return sh.as_dict()
 
     def run(self, epochs: int, batch_size: int, ns: int, lr) -> np.ndarray:
         """Trains every graph; returns the FP64 loss, shape (graphs, epochs)."""
@@ -343,14 +364,15 @@ class Batch:
 
     def autotune(self, epochs: int, batch_size: int, ns: int, lr: float):
         """Times every team shape on `epochs` real epochs (embeddings restored) and
-        keeps the fastest.  Returns ((vpw, warps, edge_cap), ms of each shape tried)."""
-        cap = 64
+        keeps the fastest.  Returns (best shape dict, [(shape dict, ms), ...])."""
+        cap = 256
         ms = np.zeros(cap, dtype=np.float32)
+        shapes = (BatchShape * cap)()
         cnt = ctypes.c_int32(0)
-        v, w, c = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
-        self._check(lib().de_batch_autotune(self._h, epochs, batch_size, ns, lr, ms.ctypes.data, cap,
-                                            ctypes.byref(cnt), ctypes.byref(v), ctypes.byref(w), ctypes.byref(c)))
-        return (v.value, w.value, c.value), ms[:cnt.value]
+        best = BatchShape()
+        self._check(lib().de_batch_autotune(self._h, epochs, batch_size, ns, lr, ms.ctypes.data, shapes, cap,
+                                            ctypes.byref(cnt), ctypes.byref(best)))
+        return best.as_dict(), [(shapes[i].as_dict(), float(ms[i])) for i in range(cnt.value)]
 
     def edge_updates(self, epochs: int, batch_size: int, ns: int) -> int:
         return int(lib().de_batch_edge_updates(self._h, epochs, batch_size, ns))

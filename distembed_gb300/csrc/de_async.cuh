@@ -1,0 +1,74 @@
+// Shared-memory barriers and bulk asynchronous copies (sm_90+ PTX), shared by the
+// kernels that stage rows through shared memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace de {
+namespace dev {
+
+// Polls of a shared-memory barrier before a wait gives up and reports an error.
+constexpr long kSpinLimit = 1L << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+// Waits for completion `parity` of the barrier; gives up after a bounded number
+// of polls, records the failure and returns false.  Returns false at once when
+// another thread has already recorded a failure.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err_shared) {
+  for (long it = 0; it < kSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*reinterpret_cast<volatile int *>(err_shared)) return false;
+  }
+  *reinterpret_cast<volatile int *>(err_shared) = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Copies `bytes` (a multiple of 16; both addresses 16-byte aligned) from global
+// memory into this CTA's shared memory; completion is counted on `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// Orders this thread's earlier generic-proxy global writes before later
+// async-proxy (bulk copy) reads issued after a barrier.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// 16-byte asynchronous copy global -> shared through L2 (LDGSTS path); both
+// addresses 16-byte aligned.  Completion: cp_async_commit / cp_async_wait.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Waits until at most N of this thread's committed groups are still in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+}  // namespace dev
+}  // namespace de

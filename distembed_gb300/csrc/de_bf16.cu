@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "de_async.cuh"
 #include "de_device.cuh"
 #include "de_internal.h"
 
@@ -36,7 +37,6 @@ using namespace dev;
 constexpr float kNearR = 0.25f;   // below this squared distance a component may clip
 constexpr int kTileRows = 128;    // rows per tcgen05 tile (M)
 constexpr int kChunk = 64;        // negatives per GEMM chunk (one 128-B swizzle atom)
-constexpr long kSpinLimit = 1L << 22;
 constexpr int kMaxKpad = 1024;    // negatives per minibatch in the BF16 form (bitmask words: 32)
 constexpr int kNearWords = kMaxKpad / 32;
 
@@ -187,8 +187,6 @@ __global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF
 
 // ------------------------------------------------------------ tcgen05 plumbing
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
 // Shared-memory matrix descriptor: K-major operand in 128-byte swizzled atoms of
 // 8 rows x 128 B (stride between 8-row groups 1024 B), sm_100 descriptor version.
 __device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
@@ -199,35 +197,6 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
 // Instruction descriptor: BF16 x BF16 -> FP32, both K-major, M x N.
 __host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-// Waits for completion `parity` of the barrier; gives up after a bounded number
-// of polls, records the failure and returns false.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err_shared) {
-  for (long it = 0; it < kSpinLimit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (*reinterpret_cast<volatile int *>(err_shared)) return false;
-  }
-  *reinterpret_cast<volatile int *>(err_shared) = 1;
-  return false;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {

@@ -162,9 +162,29 @@ int de_batch_destroy(de_batch *b);
  * concatenated in graph order (sum of n x dim). */
 int de_batch_set_embeddings_f32(de_batch *b, int32_t graph, const float *x);
 int de_batch_get_embeddings_f32(de_batch *b, int32_t graph, float *x);
-/* Team shape: vertices per warp (1, 2 or 4: a work item on 32, 16 or 8 lanes),
- * warps per team (4, 8, 16 or 32) and edge cap (1..4096). */
-int de_batch_set_shape(de_batch *b, int32_t vertices_per_warp, int32_t team_warps, int32_t edge_cap);
+/* Team shape.  Two kernel families run the same step:
+ *   DE_BATCH_REGISTER  work items read their rows into registers; a warp runs
+ *                      vertices_per_warp (1, 2 or 4) items at once on 32, 16 or 8
+ *                      lanes; team_warps 4, 8, 16 or 32; edge_cap 1..4096
+ *   DE_BATCH_STAGED    every warp stages the rows of its next stages-1 chunks in
+ *                      shared memory with bulk asynchronous copies; a pair is
+ *                      computed by dim/8 lanes; team_warps 2..16; edge_cap 1..32
+ *                      (one chunk); pairs = warp steps in flight (1 or 2);
+ *                      stages 3 or 4 ring slots per warp; at most 32 negatives
+ *                      per minibatch
+ * A shape that does not exist for the batch's dim returns DE_ERR_UNSUPPORTED. */
+#define DE_BATCH_REGISTER 0
+#define DE_BATCH_STAGED 1
+typedef struct de_batch_shape {
+  int32_t kernel;            /* DE_BATCH_*                                   */
+  int32_t vertices_per_warp; /* register kernel                              */
+  int32_t team_warps;        /* warps per team (one CTA per team)            */
+  int32_t edge_cap;          /* CSR entries per work item                    */
+  int32_t pairs;             /* staged kernel: warp steps in flight          */
+  int32_t stages;            /* staged kernel                                */
+} de_batch_shape;
+int de_batch_set_shape(de_batch *b, const de_batch_shape *shape);
+int de_batch_get_shape(const de_batch *b, de_batch_shape *shape);
 /* Trains every graph for `epochs` epochs (minibatch batch_size, ns shared
  * negatives per minibatch, lr_per_epoch[epochs]) in one launch captured in a CUDA
  * graph, and waits.  loss (nullable): [n_graphs x epochs] FP64 per-graph epoch
@@ -180,14 +200,13 @@ int de_batch_run(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, co
 int de_batch_prepare(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, const double *lr_per_epoch);
 int de_batch_launch(de_batch *b);
 int de_batch_wait(de_batch *b, double *loss);
-/* Times every team shape (vertices per warp x team warps x edge caps 32..256) on
- * `epochs` epochs of the real workload, keeps the fastest with de_batch_set_shape
- * and leaves the embeddings as they were.  ms (nullable, capacity entries):
- * the time of each shape tried, in the order vpw-major, then warps, then cap;
- * *count (nullable) receives the number tried. */
+/* Times every team shape of both kernel families on `epochs` epochs of the real
+ * workload, keeps the fastest (de_batch_set_shape) and leaves the embeddings as
+ * they were.  ms / shapes (nullable, capacity entries): the time and the shape of
+ * each one tried, in the order tried; *count (nullable): how many were tried;
+ * *best (nullable): the shape kept. */
 int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, double lr, float *ms,
-                      int32_t capacity, int32_t *count, int32_t *best_vpw, int32_t *best_warps,
-                      int32_t *best_edge_cap);
+                      de_batch_shape *shapes, int32_t capacity, int32_t *count, de_batch_shape *best);
 /* BF16 form: a pair whose squared distance computed from the BF16 copies is below
  * near_r (default 0.05) is read again from the FP32 master and recomputed; 0 turns
  * this off.  Close pairs are the ones whose distance the BF16 rounding step

@@ -58,29 +58,47 @@ def x_init(i, n, dim):
     return f32(gg.init_embedding(n, dim, seed=100 + i))
 
 
+REG = dict(kernel="register", vertices_per_warp=4, team_warps=8, edge_cap=32)
+STAGED = dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3)
+
+
 def run_batch(graphs, dim, epochs, batch, ns, lr, precision="fp32", shape=None, ids=None):
     ids = list(range(len(graphs))) if ids is None else ids
     with de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision=precision) as b:
         if shape:
-            b.set_shape(*shape)
+            b.set_shape(**shape)
         for j, (i, (_, n, _, _)) in enumerate(zip(ids, graphs)):
             b.set_embeddings(j, x_init(i, n, dim))
         loss = b.run(epochs, batch, ns, lr)
         return [b.get_embeddings(j).astype(np.float64) for j in range(len(graphs))], loss
 
 
+@pytest.mark.parametrize("kernel", ["register", "staged"])
 @pytest.mark.parametrize("dim", [32, 64, 128])
-def test_fp32_batch_matches_oracle_per_graph(dim):
+def test_fp32_batch_matches_oracle_per_graph(dim, kernel):
     E, B, ns = 3, 256, 5
     lr = [0.02 * (1 - e / E) for e in range(E)]
-    xs, loss = run_batch(GRAPHS, dim, E, B, ns, lr)
+    shape = REG if kernel == "register" else (STAGED if dim < 128 else dict(STAGED, team_warps=4, edge_cap=16))
+    xs, loss = run_batch(GRAPHS, dim, E, B, ns, lr, shape=shape)
     for i, (kind, n, rp, c) in enumerate(GRAPHS):
         xo, lo = oracle.run(rp, c, x_init(i, n, dim), E, B, ns, lr, quirks=True)
         assert rel_l2(xs[i], xo) <= RUN_REL_L2, (i, kind, n)
         assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (i, loss[i], lo)
 
 
-@pytest.mark.parametrize("shape", [(1, 4, 32), (2, 8, 8), (4, 16, 64), (4, 8, 4096), (2, 32, 128)])
+SHAPES = [dict(kernel="register", vertices_per_warp=1, team_warps=4, edge_cap=32),
+          dict(kernel="register", vertices_per_warp=2, team_warps=8, edge_cap=8),
+          dict(kernel="register", vertices_per_warp=4, team_warps=16, edge_cap=64),
+          dict(kernel="register", vertices_per_warp=4, team_warps=8, edge_cap=4096),
+          dict(kernel="register", vertices_per_warp=2, team_warps=32, edge_cap=128),
+          dict(kernel="staged", team_warps=4, edge_cap=8, pairs=1, stages=3),
+          dict(kernel="staged", team_warps=16, edge_cap=8, pairs=2, stages=3),
+          dict(kernel="staged", team_warps=12, edge_cap=16, pairs=2, stages=4),
+          dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3),
+          dict(kernel="staged", team_warps=2, edge_cap=1, pairs=1, stages=4)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "-".join(str(v) for v in s.values()))
 def test_every_team_shape_matches_oracle(shape):
     dim, E, B, ns = 64, 2, 128, 7
     xs, loss = run_batch(GRAPHS, dim, E, B, ns, 0.03, shape=shape)
@@ -90,9 +108,10 @@ def test_every_team_shape_matches_oracle(shape):
         assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (shape, i)
 
 
+@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
-def test_alone_equals_mix_bitwise(precision):
-    dim, E, B, ns, shape = 64, 3, 256, 5, (4, 8, 32)
+def test_alone_equals_mix_bitwise(precision, shape):
+    dim, E, B, ns = 64, 3, 256, 5
     xs, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision=precision, shape=shape)
     for i in (0, 3, len(GRAPHS) - 1):
         xa, la = run_batch([GRAPHS[i]], dim, E, B, ns, 0.02, precision=precision, shape=shape, ids=[i])
@@ -106,9 +125,10 @@ def test_alone_equals_mix_bitwise(precision):
         assert np.array_equal(xp[j], xs[i]) and np.array_equal(lp[j], loss[i]), i
 
 
-def test_bf16_batch_loss_within_one_percent():
+@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
+def test_bf16_batch_loss_within_one_percent(shape):
     dim, E, B, ns = 64, 4, 256, 5
-    _, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16")
+    _, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=shape)
     for i, (kind, n, rp, c) in enumerate(GRAPHS):
         x0 = x_init(i, n, dim)
         # the BF16 form starts from the BF16 rounding of the FP32 embedding
@@ -125,14 +145,17 @@ def test_autotune_keeps_embeddings_and_picks_a_valid_shape():
     with de.Batch([(rp, c) for _, _, rp, c in graphs], dim) as b:
         for i, (_, n, _, _) in enumerate(graphs):
             b.set_embeddings(i, x_init(i, n, dim))
-        (v, w, c), ms = b.autotune(1, B, ns, 0.02)
-        assert v in (1, 2, 4) and w in (4, 8, 16, 32) and c in (32, 64, 128, 256)
-        assert len(ms) == 3 * 4 * 4 and np.all(ms > 0)
+        best, tried = b.autotune(1, B, ns, 0.02)
+        assert len(tried) >= 36 and all(ms > 0 for _, ms in tried)
+        assert {sh["kernel"] for sh, _ in tried} == {0, 1}
+        assert best == min(tried, key=lambda t: t[1])[0] == b.shape()
         for i, (_, n, _, _) in enumerate(graphs):
             assert np.array_equal(b.get_embeddings(i).astype(np.float64), x_init(i, n, dim))
         loss = b.run(2, B, ns, 0.02)
         got = [b.get_embeddings(i).astype(np.float64) for i in range(len(graphs))]
-    xs, ls = run_batch(graphs, dim, 2, B, ns, 0.02, shape=(v, w, c))
+    shape = dict(best)
+    shape["kernel"] = int(shape["kernel"])
+    xs, ls = run_batch(graphs, dim, 2, B, ns, 0.02, shape=shape)
     for i in range(len(graphs)):
         assert np.array_equal(got[i], xs[i]) and np.array_equal(loss[i], ls[i])
 
@@ -183,3 +206,24 @@ def test_prepared_launch_replays_the_same_run():
         x3, _ = oracle.run(rp, c, x2, 1, B, ns, 0.02, quirks=True)
         assert rel_l2(got[i], x2) <= RUN_REL_L2
         assert rel_l2(again[i], x3) <= RUN_REL_L2
+
+
+def test_staged_rejects_more_than_32_negatives():
+    with de.Batch([(rp, c) for _, _, rp, c in GRAPHS[:2]], 64) as b:
+        b.set_shape(**STAGED)
+        with pytest.raises(de.DEError) as ei:
+            b.run(1, 256, 33, 0.02)
+        assert ei.value.code == de.DE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
+def test_hub_rows_and_many_chunks_per_warp(shape):
+    # one graph whose minibatches hold far more than 32 chunks per warp (hub rows
+    # split into cap-sized pieces), so the staged pipeline restarts within a minibatch
+    n, rp, c = gg.rmat_csr(11, 32, seed=9)
+    g = [("rmat", n, rp, c)]
+    sh = dict(shape, edge_cap=4, team_warps=2) if shape["kernel"] == "staged" else dict(shape, edge_cap=4)
+    xs, loss = run_batch(g, 32, 2, 512, 6, 0.02, shape=sh, ids=[50])
+    xo, lo = oracle.run(rp, c, x_init(50, n, 32), 2, 512, 6, 0.02, quirks=True)
+    assert rel_l2(xs[0], xo) <= RUN_REL_L2
+    assert np.all(np.abs(loss[0] - lo) <= LOSS_RTOL * lo)
