@@ -93,7 +93,7 @@ SHAPES = [dict(kernel="register", vertices_per_warp=1, team_warps=4, edge_cap=32
           dict(kernel="register", vertices_per_warp=2, team_warps=32, edge_cap=128),
           dict(kernel="staged", team_warps=4, edge_cap=8, pairs=1, stages=3),
           dict(kernel="staged", team_warps=16, edge_cap=8, pairs=2, stages=3),
-          dict(kernel="staged", team_warps=12, edge_cap=16, pairs=2, stages=4),
+          dict(kernel="staged", team_warps=8, edge_cap=16, pairs=2, stages=4),
           dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3),
           dict(kernel="staged", team_warps=2, edge_cap=1, pairs=1, stages=4)]
 
