@@ -36,7 +36,8 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version",
            "de_batch_create", "de_batch_destroy", "de_batch_set_embeddings_f32", "de_batch_get_embeddings_f32",
            "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
-           "de_batch_last_error")
+           "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
+           "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error")
 
 
 class BatchShape(ctypes.Structure):
@@ -48,6 +49,34 @@ class BatchShape(ctypes.Structure):
 
 
 BATCH_KERNEL = {"register": 0, "staged": 1}
+
+
+class JobSpec(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("rowptr", ctypes.c_void_p), ("col", ctypes.c_void_p), ("nnz", ctypes.c_int64),
+                ("dim", ctypes.c_int32), ("precision", ctypes.c_int32), ("epochs", ctypes.c_int32),
+                ("batch_size", ctypes.c_int32), ("ns", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("lr_per_epoch", ctypes.c_void_p), ("x0", ctypes.c_void_p), ("x_out", ctypes.c_void_p),
+                ("loss_out", ctypes.c_void_p)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("pad", ctypes.c_int32), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("device_bytes", ctypes.c_int64),
+                ("edge_updates", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "done", "failed", "queued", "running", "peak_running",
+                                              "budget_bytes", "reserved_bytes", "peak_reserved_bytes")]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+JOB_STATE = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
 
 class DEError(RuntimeError):
@@ -117,6 +146,17 @@ def lib():
         L.de_batch_stream.restype = _vp
         L.de_batch_last_error.argtypes = [_vp]
         L.de_batch_last_error.restype = ctypes.c_char_p
+        L.de_server_create.argtypes = [_i32, _i32, _i64, ctypes.c_double, _i32, ctypes.POINTER(_vp)]
+        L.de_server_submit.argtypes = [_vp, ctypes.POINTER(JobSpec), ctypes.POINTER(_i64)]
+        L.de_server_info.argtypes = [_vp, _i64, ctypes.POINTER(JobInfo)]
+        L.de_server_wait.argtypes = [_vp, _i64, ctypes.POINTER(JobInfo)]
+        L.de_server_drain.argtypes = [_vp]
+        L.de_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats)]
+        L.de_server_clock.argtypes = [_vp]
+        L.de_server_clock.restype = ctypes.c_double
+        L.de_server_destroy.argtypes = [_vp]
+        L.de_server_last_error.argtypes = [_vp]
+        L.de_server_last_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
 
@@ -391,6 +431,89 @@ class Batch:
         if getattr(self, "_h", None):
             lib().de_batch_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Server:
+    """The served form (de_server_*): a request loop training many jobs at once.
+
+    submit() queues a job and returns its id at once; wait(id) blocks until it is
+    done and returns (embedding, per-epoch loss, info).  The arrays of a job are
+    kept alive here until it has been waited for."""
+
+    def __init__(self, slots: int = 16, hbm_bytes: int = 0, hbm_fraction: float = 0.0, device: int = 0,
+                 quirks: bool = True):
+        L = lib()
+        h = _vp()
+        rc = L.de_server_create(device, slots, hbm_bytes, hbm_fraction, int(quirks), ctypes.byref(h))
+        if rc != DE_OK:
+            raise DEError(rc, L.de_server_last_error(None).decode())
+        self._h = h
+        self._jobs = {}
+
+    def _check(self, rc: int):
+        if rc != DE_OK:
+            raise DEError(rc, lib().de_server_last_error(self._h).decode())
+
+    def clock(self) -> float:
+        return lib().de_server_clock(self._h)
+
+    def submit(self, rowptr, col, x0, epochs: int, batch_size: int, ns: int, lr, precision: str = "fp32",
+               out=None) -> int:
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.int64) if len(col) else np.zeros(1, np.int64)
+        x0 = np.ascontiguousarray(x0, dtype=np.float32)
+        n, dim = x0.shape
+        out = np.empty((n, dim), dtype=np.float32) if out is None else out
+        loss = np.zeros(epochs, dtype=np.float64)
+        lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (epochs,)))
+        spec = JobSpec(n, rowptr.ctypes.data, col.ctypes.data, int(rowptr[-1]), dim, PRECISION[precision], epochs,
+                       batch_size, ns, 0, lrs.ctypes.data, x0.ctypes.data, out.ctypes.data, loss.ctypes.data)
+        jid = _i64(0)
+        self._check(lib().de_server_submit(self._h, ctypes.byref(spec), ctypes.byref(jid)))
+        self._jobs[jid.value] = (rowptr, col, x0, out, loss, lrs)
+        return jid.value
+
+    def info(self, jid: int) -> dict:
+        inf = JobInfo()
+        self._check(lib().de_server_info(self._h, jid, ctypes.byref(inf)))
+        d = inf.as_dict()
+        d["state"] = JOB_STATE[d["state"]]
+        return d
+
+    def wait(self, jid: int):
+        inf = JobInfo()
+        rc = lib().de_server_wait(self._h, jid, ctypes.byref(inf))
+        arrays = self._jobs.pop(jid, None)
+        self._check(rc)
+        d = inf.as_dict()
+        d["state"] = JOB_STATE[d["state"]]
+        return arrays[3], arrays[4], d
+
+    def drain(self):
+        self._check(lib().de_server_drain(self._h))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self._check(lib().de_server_get_stats(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().de_server_destroy(self._h)
+            self._h = None
+            self._jobs.clear()
 
     def __del__(self):
         try:

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/distembed_gb300.h"
+
 #include <string>
 #include <vector>
 
@@ -142,6 +144,22 @@ cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap
                               const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev);
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
 cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
+
+// Where a handle's buffers come from.  With dalloc set, device buffers come from
+// dalloc/dfree (a caller-owned arena; no implicit device synchronisation) and
+// host staging buffers from malloc; otherwise cudaMalloc and pinned cudaHostAlloc.
+struct MemHooks {
+  void *(*dalloc)(void *ctx, size_t bytes) = nullptr;
+  void (*dfree)(void *ctx, void *p) = nullptr;
+  void *ctx = nullptr;
+};
+
+// de_create with memory hooks (nullable) (de_runtime.cpp).
+int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
+                  const de_options *opts, const MemHooks *hooks, de_handle **out);
+// The FP64 per-epoch loss of the last de_run_from of `epochs` epochs; waits for
+// the handle's stream.
+int copy_loss(de_handle *h, double *out, int32_t epochs);
 
 // Launchers (de_plain.cu).  pdl: launch with a programmatic dependency on the
 // previous kernel in the stream.

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <random>
@@ -104,6 +105,9 @@ struct de_handle {
   int32_t *d_err = nullptr;
   int kpad = 0;
   CUtensorMap map_x{}, map_n{}, map_t{};
+
+  // where device and host buffers come from (default: cudaMalloc / cudaHostAlloc)
+  MemHooks hooks{};
 };
 
 namespace {
@@ -124,14 +128,55 @@ int cuda_fail(de_handle *h, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
   } while (0)
 
+// Device and host buffers of a handle: from its memory hooks when it has them
+// (a caller-owned arena: no implicit device synchronisation on free), else from
+// cudaMalloc / cudaHostAlloc (pinned).
+template <class H>
+cudaError_t dev_alloc(const H &h, void **p, size_t bytes) {
+  if (h->hooks.dalloc) {
+    *p = h->hooks.dalloc(h->hooks.ctx, bytes);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
+template <class H>
+void dev_free(const H &h, void *p) {
+  if (!p) return;
+  if (h->hooks.dalloc) {
+    // an arena block may be handed out again at once: no kernel of this
+    // handle may still be using it
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->hooks.dfree(h->hooks.ctx, p);
+  } else {
+    cudaFree(p);
+  }
+}
+
+template <class H>
+cudaError_t host_alloc(const H &h, void **p, size_t bytes) {
+  if (h->hooks.dalloc) {
+    *p = std::malloc(bytes);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+  }
+  return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
+template <class H>
+void host_free(const H &h, void *p) {
+  if (!p) return;
+  if (h->hooks.dalloc) std::free(p);
+  else cudaFreeHost(p);
+}
+
 template <typename T>
 int grow(de_handle *h, T **p, size_t *cap, size_t need, bool *moved = nullptr) {
   if (need <= *cap && *p) return DE_OK;
   size_t want = std::max(need, size_t(1));
-  if (*p) cudaFree(*p);
+  if (*p) dev_free(h, *p);
   *p = nullptr;
   *cap = 0;
-  DE_CUDA(h, cudaMalloc(reinterpret_cast<void **>(p), want * sizeof(T)));
+  DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(p), want * sizeof(T)));
   *cap = want;
   if (moved) *moved = true;
   return DE_OK;
@@ -140,11 +185,10 @@ int grow(de_handle *h, T **p, size_t *cap, size_t need, bool *moved = nullptr) {
 template <typename T>
 int grow_pinned(de_handle *h, T **p, size_t *cap, size_t need) {
   if (need <= *cap && *p) return DE_OK;
-  if (*p) cudaFreeHost(*p);
+  if (*p) host_free(h, *p);
   *p = nullptr;
   *cap = 0;
-  DE_CUDA(h, cudaHostAlloc(reinterpret_cast<void **>(p), std::max(need, size_t(1)) * sizeof(T),
-                           cudaHostAllocDefault));
+  DE_CUDA(h, host_alloc(h, reinterpret_cast<void **>(p), std::max(need, size_t(1)) * sizeof(T)));
   *cap = std::max(need, size_t(1));
   return DE_OK;
 }
@@ -210,11 +254,11 @@ int ensure_schedule(de_handle *h, int B) {
   const int cap = h->opt.edge_cap > 0 ? std::min(h->opt.edge_cap, kMaxEdgeCap) : default_edge_cap(h->dim);
   if (h->sched.batch == B && h->sched.edge_cap == cap && h->sched.d_items) return DE_OK;
   drop_graph(h);
-  if (h->sched.d_items) cudaFree(h->sched.d_items);
+  if (h->sched.d_items) dev_free(h, h->sched.d_items);
   h->sched = Schedule{};
   std::vector<WorkItem> items;
   build_schedule(h, B, cap, h->sched, items);
-  DE_CUDA(h, cudaMalloc(&h->sched.d_items, std::max<size_t>(items.size(), 1) * sizeof(WorkItem)));
+  DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->sched.d_items), std::max<size_t>(items.size(), 1) * sizeof(WorkItem)));
   DE_CUDA(h, cudaMemcpy(h->sched.d_items, items.data(), items.size() * sizeof(WorkItem),
                         cudaMemcpyHostToDevice));
   return DE_OK;
@@ -329,12 +373,12 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
   if (size_t(kpad) > h->kpad_cap || !h->d_nn) {
     for (void *p : {static_cast<void *>(h->d_nn), static_cast<void *>(h->d_nid), static_cast<void *>(h->d_nb),
                     static_cast<void *>(h->d_nbt)})
-      if (p) cudaFree(p);
+      if (p) dev_free(h, p);
     h->d_nn = nullptr; h->d_nid = nullptr; h->d_nb = nullptr; h->d_nbt = nullptr;
-    DE_CUDA(h, cudaMalloc(&h->d_nn, kpad * sizeof(float)));
-    DE_CUDA(h, cudaMalloc(&h->d_nid, kpad * sizeof(int32_t)));
-    DE_CUDA(h, cudaMalloc(&h->d_nb, size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
-    DE_CUDA(h, cudaMalloc(&h->d_nbt, size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
+    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nn), kpad * sizeof(float)));
+    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nid), kpad * sizeof(int32_t)));
+    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nb), size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
+    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nbt), size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
     h->kpad_cap = kpad;
     m = true;
   }
@@ -490,6 +534,15 @@ void de_default_options(de_options *o) {
 
 int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
               const de_options *opts, de_handle **out) {
+  return de::create_handle(n, rowptr, col, nnz, dim, opts, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace de {
+
+int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,
+                  const de_options *opts, const MemHooks *hooks, de_handle **out) {
   if (!out) return fail(nullptr, DE_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (n <= 0 || nnz < 0 || !rowptr || (nnz > 0 && !col)) return fail(nullptr, DE_ERR_INVALID, "bad graph arguments");
@@ -499,6 +552,7 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
     return fail(nullptr, DE_ERR_UNSUPPORTED, "n and nnz must be below 2^31 - 1");
   auto h = std::make_unique<de_handle>();
   if (opts) h->opt = *opts; else de_default_options(&h->opt);
+  if (hooks) h->hooks = *hooks;
   if (h->opt.precision != DE_PRECISION_FP32 && h->opt.precision != DE_PRECISION_BF16)
     return fail(nullptr, DE_ERR_INVALID, "unknown precision");
   if (h->opt.precision == DE_PRECISION_BF16 && dim < 64)
@@ -527,15 +581,15 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
     h->own_stream = true;
   }
   std::vector<int32_t> rp32(rowptr, rowptr + n + 1), col32(col, col + nnz);
-  if ((e = cudaMalloc(&h->d_rowptr, (n + 1) * sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_col, std::max<int64_t>(nnz, 1) * sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_x, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_epoch, 2 * sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_block_sums, kFlushBlocks * sizeof(double))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_done, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_err, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_flag_count, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaHostAlloc(&h->h_epoch, 2 * sizeof(int32_t), cudaHostAllocDefault)) != cudaSuccess ||
+  if ((e = dev_alloc(h, reinterpret_cast<void **>(&h->d_rowptr), (n + 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_col), std::max<int64_t>(nnz, 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_x), size_t(n) * dim * sizeof(float))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_epoch), 2 * sizeof(int32_t))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_block_sums), kFlushBlocks * sizeof(double))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_done), sizeof(int32_t))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_err), sizeof(int32_t))) != cudaSuccess ||
+      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_flag_count), sizeof(int32_t))) != cudaSuccess ||
+      (e = host_alloc(h, reinterpret_cast<void **>(&h->h_epoch), 2 * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "allocation"));
   if ((e = cudaMemcpy(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -546,8 +600,8 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
       (e = cudaMemset(h->d_flag_count, 0, sizeof(int32_t))) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "upload"));
   if (h->opt.precision == DE_PRECISION_BF16) {
-    if ((e = cudaMalloc(&h->d_xb, size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
-        (e = cudaMalloc(&h->d_loss_row, size_t(n) * sizeof(double))) != cudaSuccess ||
+    if ((e = dev_alloc(h, reinterpret_cast<void **>(&h->d_xb), size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
+        (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_loss_row), size_t(n) * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->d_xb, 0, size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
         (e = cudaMemset(h->d_loss_row, 0, size_t(n) * sizeof(double))) != cudaSuccess ||
         (e = bf16_prepare(dim)) != cudaSuccess)
@@ -557,41 +611,53 @@ int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz,
   return DE_OK;
 }
 
+int copy_loss(de_handle *h, double *out, int32_t epochs) {
+  if (!h || !out || epochs <= 0) return DE_ERR_INVALID;
+  if (size_t(epochs) > h->loss_cap || !h->d_loss) return fail(h, DE_ERR_STATE, "no loss of that many epochs");
+  DE_CUDA(h, cudaMemcpyAsync(out, h->d_loss, epochs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_device_error(h);
+}
+
+}  // namespace de
+
+extern "C" {
+
 int de_destroy(de_handle *h) {
   if (!h) return DE_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
-  cudaFree(h->d_rowptr);
-  cudaFree(h->d_col);
-  cudaFree(h->d_x);
-  cudaFree(h->sched.d_items);
-  cudaFree(h->d_stage);
-  cudaFree(h->d_parts);
-  cudaFree(h->d_counters);
-  cudaFree(h->d_loss_partial);
-  cudaFree(h->d_block_sums);
-  cudaFree(h->d_done);
-  cudaFree(h->d_err);
-  cudaFree(h->d_flag_count);
-  cudaFree(h->d_xb);
-  cudaFree(h->d_abuf);
-  cudaFree(h->d_nb);
-  cudaFree(h->d_nbt);
-  cudaFree(h->d_nn);
-  cudaFree(h->d_nid);
-  cudaFree(h->d_flag_rows);
-  cudaFree(h->d_near_bits);
-  cudaFree(h->d_loss_row);
-  cudaFree(h->d_epoch);
-  cudaFree(h->d_loss);
-  cudaFree(h->d_negs);
-  cudaFree(h->d_lr);
-  cudaFree(h->d_stage64);
-  if (h->h_negs) cudaFreeHost(h->h_negs);
-  if (h->h_lr) cudaFreeHost(h->h_lr);
-  if (h->h_loss) cudaFreeHost(h->h_loss);
-  if (h->h_epoch) cudaFreeHost(h->h_epoch);
+  dev_free(h, h->d_rowptr);
+  dev_free(h, h->d_col);
+  dev_free(h, h->d_x);
+  dev_free(h, h->sched.d_items);
+  dev_free(h, h->d_stage);
+  dev_free(h, h->d_parts);
+  dev_free(h, h->d_counters);
+  dev_free(h, h->d_loss_partial);
+  dev_free(h, h->d_block_sums);
+  dev_free(h, h->d_done);
+  dev_free(h, h->d_err);
+  dev_free(h, h->d_flag_count);
+  dev_free(h, h->d_xb);
+  dev_free(h, h->d_abuf);
+  dev_free(h, h->d_nb);
+  dev_free(h, h->d_nbt);
+  dev_free(h, h->d_nn);
+  dev_free(h, h->d_nid);
+  dev_free(h, h->d_flag_rows);
+  dev_free(h, h->d_near_bits);
+  dev_free(h, h->d_loss_row);
+  dev_free(h, h->d_epoch);
+  dev_free(h, h->d_loss);
+  dev_free(h, h->d_negs);
+  dev_free(h, h->d_lr);
+  dev_free(h, h->d_stage64);
+  if (h->h_negs) host_free(h, h->h_negs);
+  if (h->h_lr) host_free(h, h->h_lr);
+  if (h->h_loss) host_free(h, h->h_loss);
+  if (h->h_epoch) host_free(h, h->h_epoch);
   if (h->upload_done) cudaEventDestroy(h->upload_done);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;

@@ -222,6 +222,74 @@ void *de_batch_stream(de_batch *b);
 /* Text of the last error on b (NULL: of the last failed de_batch_create). */
 const char *de_batch_last_error(const de_batch *b);
 
+/* ---- Served form: a request loop that trains embedding jobs concurrently.
+ * No counterpart in the reference, which runs one job per process
+ * (cpp/dist_embed.cpp:156-347).  Each job is the one-rank step of
+ * cpp/algo/algo.hpp:164-192 on its own resident handle (FP32 plain or BF16
+ * form), so its result is the same alone or among other jobs.  Jobs are
+ * admitted in submission order when one of `slots` worker slots is free and the
+ * job's device footprint fits in the memory budget; every slot has its own CUDA
+ * stream, so the running jobs' kernels share the GPU and a job that arrives
+ * while others run starts as soon as a slot and memory free up. */
+typedef struct de_server de_server;
+
+#define DE_JOB_QUEUED 0
+#define DE_JOB_RUNNING 1
+#define DE_JOB_DONE 2
+#define DE_JOB_FAILED 3
+
+/* A job.  The arrays are the caller's and must stay valid (and x0, rowptr, col
+ * unchanged) until de_server_wait returns for the job. */
+typedef struct de_job_spec {
+  int64_t n;                  /* vertices                                        */
+  const int64_t *rowptr;      /* [n+1] CSR, columns ascending within a row       */
+  const int64_t *col;         /* [nnz]                                           */
+  int64_t nnz;
+  int32_t dim;                /* 32, 64, 128 or 256 (BF16: 64..256)              */
+  int32_t precision;          /* DE_PRECISION_*                                  */
+  int32_t epochs, batch_size, ns;
+  int32_t pad;
+  const double *lr_per_epoch; /* [epochs]                                        */
+  const float *x0;            /* [n x dim] FP32 start embedding                  */
+  float *x_out;               /* [n x dim] FP32 result                           */
+  double *loss_out;           /* nullable: [epochs] FP64 loss per epoch          */
+} de_job_spec;
+
+typedef struct de_job_info {
+  int32_t state;              /* DE_JOB_*                                        */
+  int32_t pad;
+  double submit_s, start_s, end_s; /* server clock (de_server_clock), seconds   */
+  int64_t device_bytes;       /* memory reserved for the job                     */
+  int64_t edge_updates;       /* force evaluations the job performs              */
+} de_job_info;
+
+typedef struct de_server_stats {
+  int64_t submitted, done, failed, queued, running, peak_running;
+  int64_t budget_bytes, reserved_bytes, peak_reserved_bytes;
+} de_server_stats;
+
+/* slots: jobs in flight at most.  Memory budget: hbm_bytes when > 0, else
+ * hbm_fraction (0 < f <= 1; 0: 0.8) of the device's free memory at creation,
+ * allocated once.  ref_quirks as in de_options. */
+int de_server_create(int32_t device, int32_t slots, int64_t hbm_bytes, double hbm_fraction, int32_t ref_quirks,
+                     de_server **out);
+/* Queues a job; *id identifies it.  A job larger than the whole budget returns
+ * DE_ERR_UNSUPPORTED. */
+int de_server_submit(de_server *s, const de_job_spec *job, int64_t *id);
+/* Current state of a job that has not been waited for. */
+int de_server_info(de_server *s, int64_t id, de_job_info *info);
+/* Waits until the job is done (x_out and loss_out written), returns its info
+ * and forgets it. */
+int de_server_wait(de_server *s, int64_t id, de_job_info *info);
+/* Waits until no job is queued or running. */
+int de_server_drain(de_server *s);
+int de_server_get_stats(de_server *s, de_server_stats *stats);
+/* Seconds since the server was created (the clock of de_job_info). */
+double de_server_clock(const de_server *s);
+/* Finishes the queued jobs, stops the slots and frees the budget. */
+int de_server_destroy(de_server *s);
+const char *de_server_last_error(const de_server *s);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 
