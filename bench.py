@@ -56,11 +56,13 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="max CSR entries per work item (0: automatic)")
-    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched"],
+    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched", "served"],
                    help="plain: FP32 plain form on R-MAT s20 (default line); bf16: BF16 precision form vs the "
                         "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives; batched: 512 graphs in one "
                         "persistent launch, BF16 storage, vs the FP32 plain form on the same graphs")
     p.add_argument("--graphs", type=int, default=512, help="batched form: number of graphs")
+    p.add_argument("--jobs", type=int, default=256, help="served form: jobs in the arrival stream")
+    p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
     return p.parse_args()
 
@@ -565,6 +567,145 @@ def run_batched_form(args):
     print(json.dumps(line), flush=True)
 
 
+W5 = dict(rate=200.0, seed=4, n_lo=1000, n_hi=2_000_000, dims=(32, 64, 128), epochs=(10, 50), batch=16384, ns=5,
+          lr=0.02, knn_max_n=100_000, rmat_ef=8, knn_k=10, knn_dim=32)
+
+
+def served_workload(count, device):
+    """The arrival stream: Poisson arrivals (mean W5['rate'] jobs/s), n log-uniform,
+    R-MAT or kNN (kNN only up to knn_max_n vertices: exact kNN of millions of
+    points is not generated here), dim and epochs uniform.  Every job uses the
+    reference driver's defaults for the rest (minibatch 16384, 5 negatives,
+    lr 0.02, cpp/dist_embed.cpp:46-51)."""
+    from distembed_gb300 import graphgen as gg
+    rng = np.random.Generator(np.random.PCG64(W5["seed"]))
+    arrivals = np.cumsum(rng.exponential(1.0 / W5["rate"], size=count))
+    arrivals -= arrivals[0]
+    ns_ = np.rint(np.exp(rng.uniform(np.log(W5["n_lo"]), np.log(W5["n_hi"]), size=count))).astype(np.int64)
+    kinds = rng.integers(0, 2, size=count)
+    dims = rng.choice(W5["dims"], size=count)
+    epochs = rng.integers(W5["epochs"][0], W5["epochs"][1] + 1, size=count)
+    jobs = []
+    for i in range(count):
+        n = int(ns_[i])
+        if kinds[i] == 1 and n <= W5["knn_max_n"]:
+            _, rp, col = gg.knn_csr(n, W5["knn_dim"], W5["knn_k"], 10, seed=W5["seed"] * 100003 + i, device=device)
+            kind = "knn"
+        else:
+            _, rp, col = gg.rmat_csr_torch(n, W5["rmat_ef"], seed=W5["seed"] * 100003 + i, device=device)
+            kind = "rmat"
+        jobs.append(dict(arrival=float(arrivals[i]), kind=kind, n=n, rowptr=rp, col=col, dim=int(dims[i]),
+                         epochs=int(epochs[i])))
+    return jobs
+
+
+def run_served_form(args):
+    """Served form: the arrival stream through de_server (jobs overlapping on the
+    GPU) against the FP32 plain form running the same jobs one after another."""
+    import threading
+
+    import torch
+
+    import distembed_gb300 as de
+    import oracle
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    jobs = served_workload(args.jobs, "cuda")
+    gen_s = time.perf_counter() - t0
+    B, ns, lr = W5["batch"], W5["ns"], W5["lr"]
+    nmax = max(j["n"] for j in jobs)
+    pool = np.random.Generator(np.random.PCG64(1)).uniform(-0.5, 0.5, size=nmax * 128).astype(np.float32)
+
+    def x0_of(j):  # every job starts from a slice of one seeded U[-0.5, 0.5) pool
+        return pool[: j["n"] * j["dim"]].reshape(j["n"], j["dim"])
+
+    srv = de.Server(slots=args.slots, hbm_fraction=0.85)
+    # warm-up: a few small jobs (module load, first launches)
+    small = sorted(jobs, key=lambda j: j["n"])[:4]
+    for j in small:
+        srv.wait(srv.submit(j["rowptr"], j["col"], x0_of(j), 2, B, ns, lr))
+    results = [None] * len(jobs)
+    ids = [None] * len(jobs)
+    ready = threading.Semaphore(0)
+
+    def waiter():
+        for i in range(len(jobs)):
+            ready.acquire()
+            x, loss, info = srv.wait(ids[i])
+            results[i] = (float(loss[-1]), info)
+
+    th = threading.Thread(target=waiter)
+    clocks = Clocks(0)
+    clocks.start()
+    th.start()
+    start = srv.clock() + 0.05
+    for i, j in enumerate(jobs):
+        delay = start + j["arrival"] - srv.clock()
+        if delay > 0:
+            time.sleep(delay)
+        ids[i] = srv.submit(j["rowptr"], j["col"], x0_of(j), j["epochs"], B, ns, lr)
+        ready.release()
+    th.join()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r[1]["end_s"] - (start + j["arrival"]) for r, j in zip(results, jobs)])
+    queue_wait = np.array([r[1]["start_s"] - r[1]["submit_s"] for r in results])
+    service = np.array([r[1]["end_s"] - r[1]["start_s"] for r in results])
+    upd = sum(r[1]["edge_updates"] for r in results)
+    makespan = max(r[1]["end_s"] for r in results) - start
+    value = upd / makespan
+
+    # the same jobs through the FP32 plain form, one after another (no overlap)
+    plain_s, plain_upd = 0.0, 0
+    for j in jobs:
+        with de.Handle(j["rowptr"], j["col"], j["dim"], quirks=True) as h:
+            h.set_embeddings(x0_of(j))
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            h.run(j["epochs"], B, ns, lr, want_loss=True)
+            plain_s += time.perf_counter() - t1
+            plain_upd += h.edge_updates(j["epochs"], B, ns)
+    plain_v = plain_upd / plain_s
+
+    # FP64 oracle on the three smallest kNN jobs (kNN training converges; small
+    # R-MAT jobs are chaotic, FP32 and FP64 trajectories part within tens of epochs)
+    small_knn = sorted((i for i in range(len(jobs)) if jobs[i]["kind"] == "knn"), key=lambda i: jobs[i]["n"])[:3]
+    oracle_gaps = []
+    for i in small_knn:
+        j = jobs[i]
+        _, lo = oracle.run(j["rowptr"], j["col"], x0_of(j).astype(np.float64), j["epochs"], B, ns, lr, quirks=True,
+                           threads=os.cpu_count() or 1)
+        oracle_gaps.append(abs(results[i][0] - lo[-1]) / lo[-1])
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": len(small),
+            "ms_per_step": 1e3 * makespan, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32",
+            "data": f"synthetic: {len(jobs)} jobs, Poisson arrivals {W5['rate']:.0f}/s (seed 4), n log-uniform "
+                    "[1000, 2e6], R-MAT ef 8 or kNN k=10 (kNN up to 1e5 vertices), dim in {32, 64, 128}, "
+                    "10-50 epochs; minibatch 16384, 5 negatives, lr 0.02",
+            "config": {"workload": f"served{len(jobs)}_poisson200", "jobs": len(jobs), "slots": args.slots,
+                       "step": "the whole arrival stream", "kinds": {k: sum(jj['kind'] == k for jj in jobs)
+                                                                     for k in ("knn", "rmat")},
+                       "vertices": int(sum(jj["n"] for jj in jobs)), "nnz": int(sum(len(jj["col"]) for jj in jobs)),
+                       "generate_s": round(gen_s, 1)},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max()), "queue_wait_p50": float(np.percentile(queue_wait, 50)),
+                          "service_p50": float(np.percentile(service, 50)),
+                          "service_p99": float(np.percentile(service, 99))},
+            "server": st, "edge_updates": int(upd), "makespan_s": makespan,
+            "compare": {"fp32_plain_serial": {"edge_updates_per_s": plain_v, "busy_s": plain_s},
+                        "served_over_plain": value / plain_v},
+            "loss": {"final_gap_vs_fp64_oracle_3_smallest_knn_jobs": [float(g) for g in oracle_gaps],
+                     "served_vs_alone": "bitwise equal (tests/test_gpu_served.py)"},
+            "e2e": {"value": value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(jj["n"] * jj["dim"] * 4 + len(jj["col"]) * 4 for jj in jobs)),
+                    "d2h_bytes_per_step": int(sum(jj["n"] * jj["dim"] * 4 for jj in jobs)),
+                    "note": "jobs submitted from host memory and results returned to host memory by the server"},
+            "gpu_launches": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -573,6 +714,8 @@ def main():
         run_bf16_form(args)
     elif args.form == "batched":
         run_batched_form(args)
+    elif args.form == "served":
+        run_served_form(args)
     else:
         run_ours(args)
 

@@ -922,14 +922,15 @@ int build_batched_schedule(de_batch *b, int B, int cap) {
   BCUDA(b, cudaMalloc(&b->d_bitem, bitem.size() * sizeof(int64_t)));
   BCUDA(b, cudaMalloc(&b->d_bsplit, bsplit.size() * sizeof(int32_t)));
   BCUDA(b, cudaMalloc(&b->d_splits, std::max<size_t>(splits.size(), 1) * sizeof(SplitRow)));
-  BCUDA(b, cudaMemcpy(b->d_graphs, b->ginfo.data(), b->ginfo.size() * sizeof(GraphInfo), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMemcpy(b->d_order, b->order.data(), b->order.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  BCUDA(b, cudaMemcpyAsync(b->d_graphs, b->ginfo.data(), b->ginfo.size() * sizeof(GraphInfo), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaMemcpyAsync(b->d_order, b->order.data(), b->order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
   if (!items.empty())
-    BCUDA(b, cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMemcpy(b->d_bitem, bitem.data(), bitem.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMemcpy(b->d_bsplit, bsplit.data(), bsplit.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaMemcpyAsync(b->d_bitem, bitem.data(), bitem.size() * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaMemcpyAsync(b->d_bsplit, bsplit.data(), bsplit.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
   if (!splits.empty())
-    BCUDA(b, cudaMemcpy(b->d_splits, splits.data(), splits.size() * sizeof(SplitRow), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpyAsync(b->d_splits, splits.data(), splits.size() * sizeof(SplitRow), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));  // the host vectors go away on return
   return DE_OK;
 }
 
@@ -976,9 +977,11 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   if (int rc = bgrow(b, &b->d_negs, &b->negs_cap, negs.size())) return rc;
   if (int rc = bgrow(b, &b->d_lr, &b->lr_cap, size_t(epochs))) return rc;
   if (int rc = bgrow(b, &b->d_loss, &b->loss_cap, size_t(epochs) * b->n_graphs)) return rc;
-  BCUDA(b, cudaMemcpy(b->d_negs, negs.data(), negs.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMemcpy(b->d_lr, lrf.data(), epochs * sizeof(float), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMemcpy(b->d_graphs, b->ginfo.data(), b->ginfo.size() * sizeof(GraphInfo), cudaMemcpyHostToDevice));
+  BCUDA(b, cudaMemcpyAsync(b->d_negs, negs.data(), negs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaMemcpyAsync(b->d_lr, lrf.data(), epochs * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaMemcpyAsync(b->d_graphs, b->ginfo.data(), b->ginfo.size() * sizeof(GraphInfo), cudaMemcpyHostToDevice,
+                           b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
   const int teams = teams_for(b, k);
   if (int rc = bgrow(b, &b->d_stage, &b->stage_cap, size_t(teams) * B * b->dim)) return rc;
   if (int rc = bgrow(b, &b->d_slots, &b->slots_cap, size_t(teams) * b->max_slots * b->dim)) return rc;
@@ -1092,13 +1095,16 @@ int de_batch_create(int32_t n_graphs, const int64_t *n, const int64_t *const *ro
       (e = cudaMalloc(&b->d_next, sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_trace, size_t(n_graphs) * 3 * sizeof(long long))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_err, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMemset(b->d_err, 0, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMemset(b->d_xm, 0, xn * sizeof(float))) != cudaSuccess ||
-      (!col32.empty() && (e = cudaMemcpy(b->d_col, col32.data(), col32.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess))
+      (e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), b->stream)) != cudaSuccess ||
+      (e = cudaMemsetAsync(b->d_xm, 0, xn * sizeof(float), b->stream)) != cudaSuccess ||
+      (!col32.empty() && (e = cudaMemcpyAsync(b->d_col, col32.data(), col32.size() * sizeof(int32_t),
+                                              cudaMemcpyHostToDevice, b->stream)) != cudaSuccess) ||
+      (e = cudaStreamSynchronize(b->stream)) != cudaSuccess)
     return bail(bfail(raw, e == cudaErrorMemoryAllocation ? DE_ERR_OOM : DE_ERR_CUDA, cudaGetErrorString(e)));
   if (b->opt.precision == DE_PRECISION_BF16) {
     if ((e = cudaMalloc(&b->d_xb, xn * sizeof(__nv_bfloat16))) != cudaSuccess ||
-        (e = cudaMemset(b->d_xb, 0, xn * sizeof(__nv_bfloat16))) != cudaSuccess)
+        (e = cudaMemsetAsync(b->d_xb, 0, xn * sizeof(__nv_bfloat16), b->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(b->stream)) != cudaSuccess)
       return bail(bfail(raw, e == cudaErrorMemoryAllocation ? DE_ERR_OOM : DE_ERR_CUDA, cudaGetErrorString(e)));
   }
   *out = b.release();
@@ -1199,14 +1205,16 @@ int de_batch_wait(de_batch *b, double *loss) {
   BCUDA(b, cudaSetDevice(b->device));
   BCUDA(b, cudaStreamSynchronize(b->stream));
   int32_t derr = 0;
-  BCUDA(b, cudaMemcpy(&derr, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  BCUDA(b, cudaMemcpyAsync(&derr, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
   if (derr) {
-    BCUDA(b, cudaMemset(b->d_err, 0, sizeof(int32_t)));
+    BCUDA(b, cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), b->stream));
     return bfail(b, DE_ERR_CUDA, "a bounded wait in the staged kernel gave up; results of this launch are invalid");
   }
   if (loss && b->prepared_epochs > 0)
-    BCUDA(b, cudaMemcpy(loss, b->d_loss, size_t(b->prepared_epochs) * b->n_graphs * sizeof(double),
-                        cudaMemcpyDeviceToHost));
+    BCUDA(b, cudaMemcpyAsync(loss, b->d_loss, size_t(b->prepared_epochs) * b->n_graphs * sizeof(double),
+                             cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
   return DE_OK;
 }
 
@@ -1299,7 +1307,8 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
     float t = 0.f;
     if (e == cudaSuccess && !rc) e = cudaEventElapsedTime(&t, e0, e1);
     int32_t derr = 0;
-    if (e == cudaSuccess && !rc) e = cudaMemcpy(&derr, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(&derr, b->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess && !rc) rc = bfail(b, DE_ERR_CUDA, cudaGetErrorString(e));
     if (!rc && derr) rc = bfail(b, DE_ERR_CUDA, "a bounded wait in the staged kernel gave up during tuning");
     if (rc) break;
@@ -1341,7 +1350,9 @@ int de_batch_trace(de_batch *b, int64_t *out) {
   if (!b || !out) return DE_ERR_INVALID;
   BCUDA(b, cudaSetDevice(b->device));
   BCUDA(b, cudaStreamSynchronize(b->stream));
-  BCUDA(b, cudaMemcpy(out, b->d_trace, size_t(b->n_graphs) * 3 * sizeof(long long), cudaMemcpyDeviceToHost));
+  BCUDA(b, cudaMemcpyAsync(out, b->d_trace, size_t(b->n_graphs) * 3 * sizeof(long long), cudaMemcpyDeviceToHost,
+                           b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
   return DE_OK;
 }
 

@@ -259,8 +259,11 @@ int ensure_schedule(de_handle *h, int B) {
   std::vector<WorkItem> items;
   build_schedule(h, B, cap, h->sched, items);
   DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->sched.d_items), std::max<size_t>(items.size(), 1) * sizeof(WorkItem)));
-  DE_CUDA(h, cudaMemcpy(h->sched.d_items, items.data(), items.size() * sizeof(WorkItem),
-                        cudaMemcpyHostToDevice));
+  // on the handle's stream (its kernels do not wait for the legacy stream), and
+  // finished before `items` goes away
+  DE_CUDA(h, cudaMemcpyAsync(h->sched.d_items, items.data(), items.size() * sizeof(WorkItem),
+                             cudaMemcpyHostToDevice, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
   return DE_OK;
 }
 
@@ -367,7 +370,7 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
       (rc = grow(h, &h->d_near_bits, &h->near_cap, size_t(s.batch) * 32, &near_moved)))
     return rc;
   if (near_moved) {
-    DE_CUDA(h, cudaMemset(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t)));
+    DE_CUDA(h, cudaMemsetAsync(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t), h->stream));
     m = true;
   }
   if (size_t(kpad) > h->kpad_cap || !h->d_nn) {
@@ -498,10 +501,12 @@ int capture_epoch(de_handle *h, int ns) {
 // A kernel whose bounded wait gave up records it in d_err; report and re-arm.
 int check_device_error(de_handle *h) {
   int32_t e = 0;
-  DE_CUDA(h, cudaMemcpy(&e, h->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  DE_CUDA(h, cudaMemcpyAsync(&e, h->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
   if (e) {
-    DE_CUDA(h, cudaMemset(h->d_err, 0, sizeof(int32_t)));
-    if (h->d_near_bits) DE_CUDA(h, cudaMemset(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t)));
+    DE_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(int32_t), h->stream));
+    if (h->d_near_bits) DE_CUDA(h, cudaMemsetAsync(h->d_near_bits, 0, h->near_cap * sizeof(uint32_t), h->stream));
+    DE_CUDA(h, cudaStreamSynchronize(h->stream));
     return fail(h, DE_ERR_CUDA, "a device-side wait timed out; results of this call are not valid");
   }
   return DE_OK;
@@ -592,18 +597,24 @@ int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t 
       (e = host_alloc(h, reinterpret_cast<void **>(&h->h_epoch), 2 * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "allocation"));
-  if ((e = cudaMemcpy(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (nnz > 0 && (e = cudaMemcpy(h->d_col, col32.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess) ||
-      (e = cudaMemset(h->d_x, 0, size_t(n) * dim * sizeof(float))) != cudaSuccess ||
-      (e = cudaMemset(h->d_done, 0, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMemset(h->d_err, 0, sizeof(int32_t))) != cudaSuccess ||
-      (e = cudaMemset(h->d_flag_count, 0, sizeof(int32_t))) != cudaSuccess)
+  // uploads and clears on the handle's stream: its kernels do not wait for the
+  // legacy stream, and a synchronous cudaMemcpy from pageable memory may return
+  // before its DMA has landed
+  cudaStream_t st = h->stream;
+  if ((e = cudaMemcpyAsync(h->d_rowptr, rp32.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (nnz > 0 && (e = cudaMemcpyAsync(h->d_col, col32.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice, st)) != cudaSuccess) ||
+      (e = cudaMemsetAsync(h->d_x, 0, size_t(n) * dim * sizeof(float), st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(h->d_done, 0, sizeof(int32_t), st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(h->d_err, 0, sizeof(int32_t), st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(h->d_flag_count, 0, sizeof(int32_t), st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "upload"));
   if (h->opt.precision == DE_PRECISION_BF16) {
     if ((e = dev_alloc(h, reinterpret_cast<void **>(&h->d_xb), size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
         (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_loss_row), size_t(n) * sizeof(double))) != cudaSuccess ||
-        (e = cudaMemset(h->d_xb, 0, size_t(n) * dim * sizeof(__nv_bfloat16))) != cudaSuccess ||
-        (e = cudaMemset(h->d_loss_row, 0, size_t(n) * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->d_xb, 0, size_t(n) * dim * sizeof(__nv_bfloat16), h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->d_loss_row, 0, size_t(n) * sizeof(double), h->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess ||
         (e = bf16_prepare(dim)) != cudaSuccess)
       return bail(cuda_fail(h.get(), e, "BF16 form set-up"));
   }
@@ -730,7 +741,7 @@ static int prepare_run(de_handle *h, int32_t first_epoch, int32_t epochs, int32_
       (rc = grow(h, &h->d_loss_partial, &h->loss_partial_cap, size_t(s.n_items), &moved)))
     return rc;
   if (counters_moved) {
-    DE_CUDA(h, cudaMemset(h->d_counters, 0, h->counters_cap * sizeof(int32_t)));
+    DE_CUDA(h, cudaMemsetAsync(h->d_counters, 0, h->counters_cap * sizeof(int32_t), h->stream));
     moved = true;
   }
   const size_t ecap = std::max<size_t>(size_t(epochs), 64);

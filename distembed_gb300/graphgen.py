@@ -88,6 +88,31 @@ def rmat_csr_n(n: int, edge_factor: int, seed: int, a=0.57, b=0.19, c=0.19):
     return n, *coo_to_csr(n, s, d)
 
 
+def rmat_csr_torch(n: int, edge_factor: int, seed: int, device, a=0.57, b=0.19, c=0.19):
+    """rmat_csr_n drawn with torch on `device` (input preparation for large
+    suites; its own random stream, so the graph differs from rmat_csr_n's)."""
+    import torch
+    scale = max(1, int(np.ceil(np.log2(max(n, 2)))))
+    m = edge_factor << scale
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    s = torch.zeros(m, dtype=torch.int64, device=device)
+    t = torch.zeros(m, dtype=torch.int64, device=device)
+    ab, abc = a + b, a + b + c
+    for _ in range(scale):
+        u = torch.rand(m, generator=g, device=device)
+        s = (s << 1) | (u >= ab).long()
+        t = (t << 1) | (((u >= a) & (u < ab)) | (u >= abc)).long()
+    keep = (s < n) & (t < n) & (s != t)
+    s, t = s[keep], t[keep]
+    key = torch.unique(torch.cat([s * n + t, t * n + s]))
+    rows = key // n
+    col = key - rows * n
+    rowptr = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    rowptr[1:] = torch.cumsum(torch.bincount(rows, minlength=n), 0)
+    return n, rowptr.cpu().numpy(), col.cpu().numpy()
+
+
 # ------------------------------------------------------- Gaussian-mixture kNN
 
 def gaussian_mixture(n: int, dim: int, components: int, seed: int, mean_std: float = 2.0):
@@ -119,7 +144,7 @@ def knn_edges(pts: np.ndarray, k: int, block: int = 2048):
     return src, dst
 
 
-def knn_edges_torch(pts: np.ndarray, k: int, device, block: int = 4096):
+def knn_edges_torch(pts: np.ndarray, k: int, device, block: int = 2048):
     """k nearest neighbours on a torch device in FP32 (input preparation for large
     suites; the FP64 knn_edges is the exact reference).  Self excluded."""
     import torch
