@@ -37,7 +37,8 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_batch_create", "de_batch_destroy", "de_batch_set_embeddings_f32", "de_batch_get_embeddings_f32",
            "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
            "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
-           "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error")
+           "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error",
+           "de_mm_read", "de_embedding_write")
 
 
 class BatchShape(ctypes.Structure):
@@ -157,6 +158,8 @@ def lib():
         L.de_server_destroy.argtypes = [_vp]
         L.de_server_last_error.argtypes = [_vp]
         L.de_server_last_error.restype = ctypes.c_char_p
+        L.de_mm_read.argtypes = [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _i64]
+        L.de_embedding_write.argtypes = [ctypes.c_char_p, _vp, _i64, _i32]
         _lib = L
     return _lib
 
@@ -165,6 +168,34 @@ def _ptr(a) -> int:
     if hasattr(a, "data_ptr"):
         return a.data_ptr()
     return a.ctypes.data
+
+
+DRIVER_PATH = os.path.join(HERE, "dist_embed_gb300")
+
+
+def read_mtx(path: str):
+    """MatrixMarket -> (rows, cols, rowptr, col) int64 CSR, by the library's
+    reader (cpp/io/parrallel_IO.hpp:31-88 semantics at one rank)."""
+    L = lib()
+    r, c, z = _i64(0), _i64(0), _i64(0)
+    rc = L.de_mm_read(path.encode(), ctypes.byref(r), ctypes.byref(c), ctypes.byref(z), None, None, 0)
+    if rc != DE_OK:
+        raise DEError(rc, L.de_last_error(None).decode())
+    rowptr = np.zeros(r.value + 1, dtype=np.int64)
+    col = np.zeros(max(z.value, 1), dtype=np.int64)
+    rc = L.de_mm_read(path.encode(), ctypes.byref(r), ctypes.byref(c), ctypes.byref(z), rowptr.ctypes.data,
+                      col.ctypes.data, len(col))
+    if rc != DE_OK:
+        raise DEError(rc, L.de_last_error(None).decode())
+    return r.value, c.value, rowptr, col[: z.value]
+
+
+def write_embedding(path: str, x) -> None:
+    """The reference's embedding file (cpp/io/parrallel_IO.hpp:90-146)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    rc = lib().de_embedding_write(path.encode(), x.ctypes.data, x.shape[0], x.shape[1])
+    if rc != DE_OK:
+        raise DEError(rc, lib().de_last_error(None).decode())
 
 
 def negatives(n: int, seed: int, ns: int) -> np.ndarray:

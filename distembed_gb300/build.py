@@ -3,7 +3,8 @@
     python -m distembed_gb300.build [--force]
 
 Each translation unit under csrc/ is compiled by nvcc in parallel, then linked
-into one shared library next to this file.  The library links only the CUDA
+into one shared library next to this file; the host driver (driver/) is then
+compiled by the C++ compiler against it.  The library links only the CUDA
 runtime (and, for the tensor-map driver call, nothing else: the driver entry
 point is fetched at run time).
 """
@@ -20,6 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdistembed_gb300.so")
+DRIVER_SRC = os.path.join(HERE, "driver", "dist_embed_gb300.cpp")
+DRIVER = os.path.join(HERE, "dist_embed_gb300")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I" + os.path.join(HERE, "..", "include")]
@@ -72,6 +75,14 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # the host driver (C++ only: links the library, finds it next to itself)
+    if force or _stale(DRIVER, [DRIVER_SRC, LIB] + _headers()):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(HERE, "..", "include"), DRIVER_SRC, "-L" + HERE,
+               "-ldistembed_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(LIB)
     return LIB

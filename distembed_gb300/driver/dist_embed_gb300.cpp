@@ -1,0 +1,151 @@
+// dist_embed_gb300 — the reference's host driver (cpp/dist_embed.cpp) for the
+// force-model embedding branch (cpp/dist_embed.cpp:330-347), on one GB300.
+//
+// Same flags, same input (MatrixMarket, cpp/io/parrallel_IO.hpp:31-88), same
+// initial embedding (DenseMat, cpp/core/dense_mat.hpp:55-63: U[-1, 1) from the
+// C library's rand(), unseeded), same entry (EmbeddingAlgo::algo_force2_vec_ns
+// through GpuEmbeddingAlgo) and same output file (<output>/embedding.txt,
+// cpp/io/parrallel_IO.hpp:90-146).  Extra flags: -dim (the reference fixes 128
+// at compile time), -precision fp32|bf16, -device.  Flags that select other
+// algorithms of the reference (-spmm, -spgemm, -sparse_embedding, -msbfs) are
+// refused; flags of the multi-rank exchange are accepted and not used.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "distembed_gb300.hpp"
+
+namespace {
+
+// The one-rank shapes the reference's EmbeddingAlgo constructor reads.
+struct CSRHandle {
+  std::vector<int64_t> rowStart, col_idx;
+};
+struct CSRLocal {
+  std::unique_ptr<CSRHandle> handler = std::make_unique<CSRHandle>();
+};
+struct SpMat {
+  std::unique_ptr<CSRLocal> csr_local_data = std::make_unique<CSRLocal>();
+  int64_t gRows = 0, gCols = 0, gNNz = 0;
+};
+struct DenseMat {
+  uint64_t rows = 0;
+  double *nCoordinates = nullptr;
+};
+struct Grid {};
+
+struct Flags {
+  std::string input, output = "embedding.txt", dataset;
+  int batch_size = 16384, iterations = 30, ns = 5, dim = 128, device = 0;
+  double alpha = 0, beta = 0.25, lr = 0.02;
+  bool col_major = false, sync_comm = false;
+  int precision = DE_PRECISION_FP32;
+};
+
+template <size_t D>
+double run(const Flags &f, SpMat &sp, DenseMat &dense, std::vector<double> &loss) {
+  Grid grid;
+  distembed_gb300::GpuEmbeddingAlgo<int64_t, double, D> algo(&sp, &sp, &sp, &dense, &grid, f.alpha, f.beta, 5.0, -5.0,
+                                                             f.col_major, f.sync_comm, f.precision, f.device);
+  const auto t0 = std::chrono::steady_clock::now();
+  algo.algo_force2_vec_ns(f.iterations, f.batch_size, f.ns, f.lr);
+  const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  loss = algo.last_loss();
+  return s;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  Flags f;
+  for (int p = 0; p + 1 < argc; p++) {
+    const char *a = argv[p], *v = argv[p + 1];
+    if (!std::strcmp(a, "-input")) f.input = v;
+    else if (!std::strcmp(a, "-output")) f.output = v;
+    else if (!std::strcmp(a, "-batch")) f.batch_size = std::atoi(v);
+    else if (!std::strcmp(a, "-iter")) f.iterations = std::atoi(v);
+    else if (!std::strcmp(a, "-alpha")) f.alpha = std::atof(v);
+    else if (!std::strcmp(a, "-lr")) f.lr = std::atof(v);
+    else if (!std::strcmp(a, "-nsamples")) f.ns = std::atoi(v);
+    else if (!std::strcmp(a, "-beta")) f.beta = std::atof(v);
+    else if (!std::strcmp(a, "-dataset")) f.dataset = v;
+    else if (!std::strcmp(a, "-col_major")) f.col_major = std::atoi(v) != 0;
+    else if (!std::strcmp(a, "-sync_comm")) f.sync_comm = std::atoi(v) != 0;
+    else if (!std::strcmp(a, "-dim")) f.dim = std::atoi(v);
+    else if (!std::strcmp(a, "-device")) f.device = std::atoi(v);
+    else if (!std::strcmp(a, "-precision")) f.precision = std::strcmp(v, "bf16") ? DE_PRECISION_FP32 : DE_PRECISION_BF16;
+    else if ((!std::strcmp(a, "-spmm") || !std::strcmp(a, "-spgemm") || !std::strcmp(a, "-sparse_embedding") ||
+              !std::strcmp(a, "-msbfs")) && std::atoi(v) == 1) {
+      std::fprintf(stderr, "%s: only the force-model embedding is provided by this build\n", a);
+      return 2;
+    }
+  }
+  if (f.input.empty()) {
+    std::fprintf(stderr, "usage: %s -input graph.mtx [-output dir] [-iter 30] [-batch 16384] [-nsamples 5] "
+                         "[-lr 0.02] [-dim 128] [-precision fp32|bf16] [-device 0]\n", argv[0]);
+    return 2;
+  }
+  // ---- input (cpp/dist_embed.cpp:165)
+  SpMat sp;
+  int64_t rows = 0, cols = 0, nnz = 0;
+  if (de_mm_read(f.input.c_str(), &rows, &cols, &nnz, nullptr, nullptr, 0) != DE_OK) {
+    std::fprintf(stderr, "reading %s: %s\n", f.input.c_str(), de_last_error(nullptr));
+    return 1;
+  }
+  if (cols > rows) {
+    std::fprintf(stderr, "the graph has more columns (%lld) than rows (%lld)\n", (long long)cols, (long long)rows);
+    return 1;
+  }
+  CSRHandle &csr = *sp.csr_local_data->handler;
+  csr.rowStart.resize(size_t(rows) + 1);
+  csr.col_idx.resize(size_t(nnz > 0 ? nnz : 1));
+  if (de_mm_read(f.input.c_str(), &rows, &cols, &nnz, csr.rowStart.data(), csr.col_idx.data(), int64_t(csr.col_idx.size())) !=
+      DE_OK) {
+    std::fprintf(stderr, "reading %s: %s\n", f.input.c_str(), de_last_error(nullptr));
+    return 1;
+  }
+  sp.gRows = rows;
+  sp.gCols = cols;
+  sp.gNNz = nnz;
+  std::printf(" rank 0 gROWs  %lld gCols %lld nnz %lld\n", (long long)rows, (long long)cols, (long long)nnz);
+  // ---- initial embedding (cpp/core/dense_mat.hpp:55-63)
+  std::vector<double> coords(size_t(rows) * size_t(f.dim));
+  for (size_t i = 0; i < coords.size(); ++i) coords[i] = -1.0 + 2.0 * std::rand() / (RAND_MAX + 1.0);
+  DenseMat dense;
+  dense.rows = uint64_t(rows);
+  dense.nCoordinates = coords.data();
+  // ---- the algorithm (cpp/dist_embed.cpp:331-344)
+  std::vector<double> loss;
+  double secs = 0;
+  try {
+    switch (f.dim) {
+      case 32: secs = run<32>(f, sp, dense, loss); break;
+      case 64: secs = run<64>(f, sp, dense, loss); break;
+      case 128: secs = run<128>(f, sp, dense, loss); break;
+      case 256: secs = run<256>(f, sp, dense, loss); break;
+      default: std::fprintf(stderr, "-dim must be 32, 64, 128 or 256\n"); return 2;
+    }
+  } catch (const distembed_gb300::Error &e) {
+    std::fprintf(stderr, "embedding failed: %s\n", e.what());
+    return 1;
+  }
+  std::printf(" rank 0 algo completed in %.3f s, final loss %.6e\n", secs, loss.empty() ? 0.0 : loss.back());
+  // ---- output (cpp/dist_embed.cpp:346)
+  const std::string out = f.output + "/embedding.txt";
+  if (de_embedding_write(out.c_str(), coords.data(), rows, f.dim) != DE_OK) {
+    std::fprintf(stderr, "writing %s: %s\n", out.c_str(), de_last_error(nullptr));
+    return 1;
+  }
+  // ---- timing record (the reference appends its perf JSON to "perf_output")
+  if (FILE *pf = std::fopen("perf_output", "a")) {
+    std::fprintf(pf, "{\"alpha\":%g,\"beta\":%g,\"algo\":\"Embedding\",\"p\":1,\"data_set\":\"%s\",\"device\":\"GB300\","
+                     "\"total_time_s\":%.6f,\"iterations\":%d,\"batch\":%d,\"ns\":%d}\n",
+                 f.alpha, f.beta, f.dataset.c_str(), secs, f.iterations, f.batch_size, f.ns);
+    std::fclose(pf);
+  }
+  return 0;
+}

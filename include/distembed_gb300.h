@@ -290,6 +290,18 @@ double de_server_clock(const de_server *s);
 int de_server_destroy(de_server *s);
 const char *de_server_last_error(const de_server *s);
 
+/* ---- Input and output of the driver (host only, no GPU needed).
+ * MatrixMarket reader with the semantics of ParallelIO::parallel_read_MM
+ * (cpp/io/parrallel_IO.hpp:31-88) at one rank: coordinate format, 1-based,
+ * duplicates merged, values ignored, a symmetric header mirrors off-diagonal
+ * entries; CSR columns ascending.  Call with rowptr = col = NULL for the sizes
+ * (rows, cols, nnz after merging), then with rowptr[rows+1], col[capacity >= nnz]. */
+int de_mm_read(const char *path, int64_t *rows, int64_t *cols, int64_t *nnz, int64_t *rowptr, int64_t *col,
+               int64_t capacity);
+/* Embedding writer of ParallelIO::parallel_write (cpp/io/parrallel_IO.hpp:90-146):
+ * per row "%lu" (1-based id), dim times " %.5f", "\n"; no header. */
+int de_embedding_write(const char *path, const double *x, int64_t rows, int32_t dim);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 

@@ -1,0 +1,70 @@
+"""The host driver end to end on the GPU: MatrixMarket in, the reference's
+initial embedding (U[-1, 1) from the C library's unseeded rand(),
+cpp/core/dense_mat.hpp:55-63), the epochs through GpuEmbeddingAlgo, the
+reference's embedding file out.
+
+Tolerance: the file holds 5 decimals, so every value must be within 6e-6 of the
+same run through the Python API (identical GPU arithmetic), and the embedding
+within the FP32 plain run tolerance of the FP64 oracle
+(||x - x_oracle|| / ||x_oracle|| <= 1e-4).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import distembed_gb300 as de
+import oracle
+from distembed_gb300 import graphgen as gg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from distembed_gb300 import build
+    build.build()
+
+
+def reference_init(n, dim):
+    """DenseMat's initial values: -1 + 2 rand() / (RAND_MAX + 1), row-major, glibc
+    rand() from its default seed."""
+    libc = ctypes.CDLL(None)
+    libc.srand(1)
+    vals = np.array([libc.rand() for _ in range(n * dim)], dtype=np.float64)
+    return (-1.0 + 2.0 * vals / (2147483647 + 1.0)).reshape(n, dim)
+
+
+def read_embedding(path, dim):
+    rows = [line.split() for line in open(path)]
+    ids = np.array([int(r[0]) for r in rows])
+    x = np.array([[float(v) for v in r[1:]] for r in rows])
+    assert x.shape[1] == dim
+    return ids, x
+
+
+@pytest.mark.parametrize("dim", [64, 128])
+def test_driver_matches_api_and_oracle(tmp_path, dim):
+    n, rp, col = gg.knn_csr(1500, 16, 8, 5, seed=90 + dim)
+    mtx = str(tmp_path / "g.mtx")
+    gg.write_mtx(mtx, n, rp, col)
+    out = tmp_path / "out"
+    out.mkdir()
+    E, B, ns, lr = 4, 256, 5, 0.02
+    r = subprocess.run([de.DRIVER_PATH, "-input", mtx, "-output", str(out), "-iter", str(E), "-batch", str(B),
+                        "-nsamples", str(ns), "-lr", str(lr), "-dim", str(dim)], capture_output=True, text=True,
+                       cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    ids, x = read_embedding(str(out / "embedding.txt"), dim)
+    assert np.array_equal(ids, np.arange(1, n + 1))
+    x0 = reference_init(n, dim)
+    with de.Handle(rp, col, dim) as h:
+        h.set_embeddings(x0)
+        h.run(E, B, ns, lr)
+        xa = h.get_embeddings()
+    assert np.max(np.abs(x - xa)) <= 6e-6
+    xo, _ = oracle.run(rp, col, x0, E, B, ns, lr, quirks=True)
+    assert np.linalg.norm(xa - xo) / np.linalg.norm(xo) <= 1e-4
+    assert os.path.exists(tmp_path / "perf_output")

@@ -1,0 +1,101 @@
+"""MatrixMarket reader, embedding writer and the host driver, without a GPU.
+
+The reader follows ParallelIO::parallel_read_MM at one rank
+(cpp/io/parrallel_IO.hpp:31-88): 1-based coordinates, duplicates merged, values
+ignored, a symmetric header mirrors off-diagonal entries.  The writer follows
+ParallelIO::parallel_write (cpp/io/parrallel_IO.hpp:90-146).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import distembed_gb300 as de
+from distembed_gb300 import graphgen as gg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from distembed_gb300 import build
+    build.build()
+
+
+def test_reader_round_trips_the_generators_files(tmp_path):
+    n, rp, col = gg.knn_csr(300, 8, 6, 3, seed=2)
+    p = str(tmp_path / "g.mtx")
+    gg.write_mtx(p, n, rp, col)
+    r, c, rp2, col2 = de.read_mtx(p)
+    assert (r, c) == (n, n)
+    assert np.array_equal(rp2, rp) and np.array_equal(col2, col)
+    # the Python reader agrees
+    n3, m3, rp3, col3 = gg.read_mtx(p)
+    assert n3 == m3 == n and np.array_equal(rp3, rp) and np.array_equal(col3, col)
+
+
+def test_reader_mirrors_symmetric_files_and_merges_duplicates(tmp_path):
+    p = str(tmp_path / "s.mtx")
+    with open(p, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate real symmetric\n% a comment\n5 5 6\n"
+                "2 1 1.0\n3 1 2.5\n3 3 1.0\n5 4 7\n2 1 9.0\n4 2 0.5\n")
+    r, c, rp, col = de.read_mtx(p)
+    want = {(1, 0), (0, 1), (2, 0), (0, 2), (2, 2), (4, 3), (3, 4), (3, 1), (1, 3)}
+    got = {(i, int(col[e])) for i in range(r) for e in range(rp[i], rp[i + 1])}
+    assert (r, c) == (5, 5) and got == want
+    for i in range(r):  # ascending columns within a row
+        assert np.all(np.diff(col[rp[i]:rp[i + 1]]) > 0)
+
+
+def test_reader_rejects_bad_files(tmp_path):
+    bad = tmp_path / "b.mtx"
+    bad.write_text("%%MatrixMarket matrix array real general\n2 2\n1\n2\n3\n4\n")
+    with pytest.raises(de.DEError):
+        de.read_mtx(str(bad))
+    bad.write_text("%%MatrixMarket matrix coordinate pattern general\n3 3 2\n1 2\n4 1\n")
+    with pytest.raises(de.DEError):
+        de.read_mtx(str(bad))
+    with pytest.raises(de.DEError):
+        de.read_mtx(str(tmp_path / "missing.mtx"))
+
+
+def test_writer_format(tmp_path):
+    x = np.array([[0.5, -1.25, 3.0], [1e-7, 2.0 / 3.0, -0.000004]])
+    p = str(tmp_path / "e.txt")
+    de.write_embedding(p, x)
+    want = "".join(f"{i + 1}" + "".join(f" {v:.5f}" for v in row) + "\n" for i, row in enumerate(x))
+    assert open(p).read() == want
+
+
+def test_driver_usage_and_missing_input_without_a_gpu(tmp_path):
+    exe = de.DRIVER_PATH
+    assert os.access(exe, os.X_OK)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exe, "-input", str(tmp_path / "none.mtx")], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    r = subprocess.run([exe, "-input", "x.mtx", "-spmm", "1"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+def test_cpp_header_compiles_against_reference_shaped_types(tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text('''
+#include <memory>
+#include <vector>
+#include "distembed_gb300.hpp"
+struct CSRHandle { std::vector<long long> rowStart, col_idx; };
+struct CSRLocal { std::unique_ptr<CSRHandle> handler; };
+struct SpMat { std::unique_ptr<CSRLocal> csr_local_data; };
+struct DenseMat { unsigned long rows; double *nCoordinates; };
+struct Grid {};
+using Algo = distembed_gb300::GpuEmbeddingAlgo<long long, double, 128>;
+void f(SpMat *s, DenseMat *d, Grid *g) {
+  Algo a(s, s, s, d, g, 0.0, 0.25, 5.0, -5.0, false, false);
+  a.algo_force2_vec_ns(30, 16384, 5, 0.02);
+}
+''')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
