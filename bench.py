@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--jobs", type=int, default=256, help="served form: jobs in the arrival stream")
     p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
+    p.add_argument("--shape", default="", help="batched form: team shape instead of the autotuner, "
+                                               "staged:W:cap:steps:stages or register:vpw:W:cap")
     return p.parse_args()
 
 
@@ -436,7 +438,15 @@ def run_batched_form(args):
     stream = torch.cuda.ExternalStream(b.stream, device=0)
     b.set_embeddings(-1, x0_all)
     t0 = time.perf_counter()
-    shape, tuned = b.autotune(1, B, ns, lr)
+    if args.shape:
+        f = args.shape.split(":")
+        if f[0] == "staged":
+            b.set_shape(kernel="staged", team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]))
+        else:
+            b.set_shape(kernel="register", vertices_per_warp=int(f[1]), team_warps=int(f[2]), edge_cap=int(f[3]))
+        shape, tuned = b.shape(), []
+    else:
+        shape, tuned = b.autotune(1, B, ns, lr)
     tune_s = time.perf_counter() - t0
     upd = b.edge_updates(E, B, ns)
     b.prepare(E, B, ns, lr)
@@ -444,22 +454,28 @@ def run_batched_form(args):
     b.set_embeddings(-1, x0_all)
     b.launch()
     loss_bf16 = b.wait()
+    # every step is the same job: embeddings back to the start values (untimed),
+    # then the one launch (timed with events on the batch's stream)
+    x_start = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+    x_start[:] = x0_all
     for _ in range(args.warmup):
+        b.set_embeddings(-1, x_start)
         b.launch()
-    b.wait()
+        b.wait()
     clocks = Clocks(0)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
-    ev[0].record(stream)
     for k in range(args.steps):
+        b.set_embeddings(-1, x_start)
+        ev[2 * k].record(stream)
         b.launch()
-        ev[k + 1].record(stream)
-    b.wait()
+        ev[2 * k + 1].record(stream)
+        b.wait()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    step_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
     total_s = sum(step_ms) / 1e3
     value = upd * args.steps / total_s
 
@@ -487,7 +503,10 @@ def run_batched_form(args):
 
     # FP32 storage in the same batched launch: the loss the BF16 storage is held to
     bf = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="fp32")
-    bf.set_shape(**shape)
+    try:
+        bf.set_shape(**shape)
+    except de.DEError:  # the shape's FP32 rows do not fit in shared memory: the autotuner picks one
+        bf.autotune(1, B, ns, lr)
     bf.set_embeddings(-1, x0_all)
     loss_fp32 = bf.run(E, B, ns, lr)
     bf.close()
@@ -549,6 +568,7 @@ def run_batched_form(args):
             "data": f"synthetic: {len(graphs)} graphs, n log-uniform [500, 50000] (seed 3), even: kNN k=10 of 32-D "
                     "10-component mixtures, odd: R-MAT ef 8; U[-0.5,0.5] init (seed 1000+i)",
             "config": {"workload": f"batched{len(graphs)}_d64_b256_ns5_e20_bf16", "graphs": len(graphs),
+                       "reset": "embeddings reset to the start values before every step (untimed)",
                        "vertices": total_n, "nnz": total_nnz, "dim": dim, "batch": B, "ns": ns, "lr": lr,
                        "epochs_per_job": E, "step": "one launch: every graph, 20 epochs (CUDA graph)",
                        "l2": f"inputs larger than L2 ({total_n * dim * 6 / 2**30:.2f} GiB of embeddings); no flush",

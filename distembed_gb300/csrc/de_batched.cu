@@ -825,7 +825,7 @@ struct de_batch {
   BatchedArgs args{};
   cudaGraphExec_t exec = nullptr;  // the prepared run
   int prepared_epochs = 0;
-  float near_r = 0.05f;            // BF16 form: squared distance below which a pair is recomputed in FP32
+  float near_r = 0.02f;            // BF16 form: squared distance below which a pair is recomputed in FP32
   long long *d_trace = nullptr;    // [n_graphs x 3] of the last launch
 };
 

@@ -208,7 +208,7 @@ int de_batch_wait(de_batch *b, double *loss);
 int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t ns, double lr, float *ms,
                       de_batch_shape *shapes, int32_t capacity, int32_t *count, de_batch_shape *best);
 /* BF16 form: a pair whose squared distance computed from the BF16 copies is below
- * near_r (default 0.05) is read again from the FP32 master and recomputed; 0 turns
+ * near_r (default 0.02) is read again from the FP32 master and recomputed; 0 turns
  * this off.  Close pairs are the ones whose distance the BF16 rounding step
  * distorts. */
 int de_batch_set_near_distance(de_batch *b, float near_r);
