@@ -73,6 +73,21 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(seconds: float, world: int) -> float:
+    """The slowest rank's time (the whole job ends when the last replica does)."""
+    if world <= 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t[0])
+
+
+def whole_job_rate(units_per_rank: int, seconds: float, world: int) -> float:
+    """Replicas: every rank does the same units; value = all ranks' units / slowest time."""
+    return units_per_rank * world / max_over_ranks(seconds, world)
+
+
 def workload():
     from distembed_gb300 import graphgen as gg
     n, rowptr, col = gg.rmat_csr(W["scale"], W["edge_factor"], seed=W["seed"])
@@ -246,13 +261,8 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     step_ms = [events[k].elapsed_time(events[k + 1]) for k in range(args.steps)]
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t[0])
-    units = sum(upd[k % E] for k in range(args.steps)) * world
-    value = units / total_s
+    total_s = max_over_ranks(sum(step_ms) / 1e3, world)
+    value = whole_job_rate(sum(upd[k % E] for k in range(args.steps)), total_s, world)
 
     # roofline of the dominant kernel (the per-minibatch kernel: all but one
     # launch of an epoch); per launch = epoch time / launches, gaps included
@@ -284,11 +294,7 @@ def run_ours(args):
             if k > 0:
                 e2e_times.append(t1 - t0)
         e2e_units = sum(upd) * world
-        e2e_s = statistics.mean(e2e_times)
-        if world > 1:
-            t = torch.tensor([e2e_s], dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t[0])
+        e2e_s = max_over_ranks(statistics.mean(e2e_times), world)
         h2d = n * dim * 8 + E * batches * ns * 4 + E * 4 + 8
         d2h = n * dim * 8 + E * 8
         e2e = {"value": e2e_units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
