@@ -62,10 +62,11 @@ def parse():
                         "persistent launch, BF16 storage, vs the FP32 plain form on the same graphs")
     p.add_argument("--graphs", type=int, default=512, help="batched form: number of graphs")
     p.add_argument("--jobs", type=int, default=256, help="served form: jobs in the arrival stream")
+    p.add_argument("--scale", type=int, default=0, help="bf16 form: R-MAT scale instead of 22 (small profiling cases)")
     p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
     p.add_argument("--shape", default="", help="batched form: team shape instead of the autotuner, "
-                                               "staged:W:cap:steps:stages or register:vpw:W:cap")
+                                               "staged|rows:W:cap:steps:stages or register:vpw:W:cap")
     return p.parse_args()
 
 
@@ -364,7 +365,8 @@ def run_bf16_form(args):
     from distembed_gb300 import graphgen as gg
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    n, rowptr, col = gg.rmat_csr(W3["scale"], W3["edge_factor"], seed=W3["seed"])
+    scale = args.scale or W3["scale"]
+    n, rowptr, col = gg.rmat_csr(scale, W3["edge_factor"], seed=W3["seed"])
     x0 = gg.init_embedding(n, W3["dim"], seed=W3["init_seed"]).astype(np.float32)
     gen_s = time.perf_counter() - t0
     dim, B, ns, lr, E = W3["dim"], W3["batch"], W3["ns"], W3["lr"], W3["epochs"]
@@ -388,7 +390,7 @@ def run_bf16_form(args):
             "warmup": 1, "ms_per_step": out["bf16"]["ms_per_epoch"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic: R-MAT scale 22 (ef 16, a.57 b.19 c.19, seed 2), U[-0.5,0.5] init (seed 0)",
-            "config": {"workload": WORKLOAD3 + "_bf16", "n": n, "nnz": int(len(col)), "dim": dim, "batch": B,
+            "config": {"workload": (WORKLOAD3 if scale == W3["scale"] else f"rmat{scale}_ef16_d256_b8192_ns1024") + "_bf16", "n": n, "nnz": int(len(col)), "dim": dim, "batch": B,
                        "ns": ns, "lr": lr, "epochs_per_job": E, "step": "one epoch (512 minibatches)",
                        "generate_s": round(gen_s, 1)},
             "compare": {"fp32_plain": {k: v for k, v in out["fp32"].items()}, "bf16": out["bf16"],
@@ -446,8 +448,8 @@ def run_batched_form(args):
     t0 = time.perf_counter()
     if args.shape:
         f = args.shape.split(":")
-        if f[0] == "staged":
-            b.set_shape(kernel="staged", team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]))
+        if f[0] in ("staged", "rows"):
+            b.set_shape(kernel=f[0], team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]))
         else:
             b.set_shape(kernel="register", vertices_per_warp=int(f[1]), team_warps=int(f[2]), edge_cap=int(f[3]))
         shape, tuned = b.shape(), []

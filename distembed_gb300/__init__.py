@@ -49,7 +49,7 @@ class BatchShape(ctypes.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
-BATCH_KERNEL = {"register": 0, "staged": 1}
+BATCH_KERNEL = {"register": 0, "staged": 1, "rows": 2}
 
 
 class JobSpec(ctypes.Structure):
@@ -400,7 +400,7 @@ class Batch:
         return out
 
     def set_shape(self, kernel="register", vertices_per_warp=0, team_warps=8, edge_cap=32, pairs=0, stages=0):
-        """Team shape (see de_batch_shape); kernel "register" or "staged" (or 0 / 1)."""
+        """Team shape (see de_batch_shape); kernel "register", "staged" or "rows" (or 0 / 1 / 2)."""
         k = BATCH_KERNEL.get(kernel, kernel)
         sh = BatchShape(k, vertices_per_warp, team_warps, edge_cap, pairs, stages)
         self._check(lib().de_batch_set_shape(self._h, ctypes.byref(sh)))

@@ -22,717 +22,15 @@
 #include <string>
 #include <vector>
 
-#include "../../include/distembed_gb300.h"
-#include "de_async.cuh"
-#include "de_device.cuh"
-#include "de_internal.h"
+#include "de_batched.cuh"
 
 namespace de {
 void set_thread_error(const std::string &msg);  // de_runtime.cpp
 }
 
+using namespace de::batched;
+
 namespace {
-
-using de::WorkItem;
-namespace dev = de::dev;
-
-constexpr unsigned kAll = 0xffffffffu;
-
-struct GraphInfo {
-  int64_t voff;      // first vertex of the graph in the concatenated embedding
-  int64_t eoff;      // first CSR entry of the graph in the concatenated col array
-  int64_t batch_off; // first minibatch of the graph in the per-minibatch tables
-  int64_t neg_off;   // first negative of the graph (per run: [epochs, batches, ns])
-  int32_t n, batches, last_batch_size;
-  int32_t pad;
-};
-
-struct SplitRow {
-  int32_t row, first_slot, nparts, pad;
-};
-
-struct BatchedArgs {
-  const GraphInfo *graphs;
-  const int32_t *order;      // graphs, largest first
-  int32_t n_graphs;
-  int32_t *next_graph;       // team work counter, zeroed before the launch
-  const int32_t *col;        // every graph's CSR columns, concatenated (graph g from eoff)
-  const WorkItem *items;     // rows are local to the minibatch, edges local to the graph
-  const int64_t *batch_item_off;
-  const int32_t *batch_split_off;
-  const SplitRow *splits;
-  float *xm;                 // FP32 master [sum n, dim]
-  __nv_bfloat16 *xb;         // BF16 copy (BF16 form) or nullptr
-  const int32_t *negs;       // [graph][epoch][batch][ns]
-  const float *lr;           // [epochs]
-  int32_t epochs, batch, ns, quirks, compute_loss;
-  float bound;
-  float *stage;              // [teams, batch, dim] staged updates
-  float *slots;              // [teams, max slots, dim] partials of split rows
-  int32_t slot_stride;       // slots per team
-  double *loss;              // [n_graphs, epochs]
-  float near_r;              // BF16 form: pairs closer than this are recomputed in FP32
-  long long *trace;          // nullable: per graph {start ns, end ns, team}
-  int32_t cap;               // staged kernel: CSR entries per chunk (<= 32)
-  int32_t *err;              // staged kernel: set when a bounded wait gives up
-};
-
-// One group of L = 32 / VPW lanes works on one item; lane j of the group holds
-// components [j*P, j*P + P) of a row, P = D / L.
-template <int D, int VPW>
-struct Row {
-  static constexpr int L = 32 / VPW;
-  static constexpr int P = D / L;
-  float v[P];
-};
-
-template <int D, int VPW, bool kBF16>
-__device__ __forceinline__ void load_row(Row<D, VPW> &r, const BatchedArgs &a, int64_t vertex, int gl) {
-  constexpr int P = Row<D, VPW>::P;
-  const int64_t base = vertex * D + int64_t(gl) * P;
-  if constexpr (kBF16) {
-    const __nv_bfloat162 *p = reinterpret_cast<const __nv_bfloat162 *>(a.xb + base);
-#pragma unroll
-    for (int i = 0; i < P / 2; ++i) {
-      float2 f = __bfloat1622float2(p[i]);
-      r.v[2 * i] = f.x;
-      r.v[2 * i + 1] = f.y;
-    }
-  } else {
-    const float2 *p = reinterpret_cast<const float2 *>(a.xm + base);
-#pragma unroll
-    for (int i = 0; i < P / 2; ++i) {
-      float2 f = __ldcg(p + i);
-      r.v[2 * i] = f.x;
-      r.v[2 * i + 1] = f.y;
-    }
-  }
-}
-
-template <int L>
-__device__ __forceinline__ float group_sum(float v) {
-#pragma unroll
-  for (int m = L / 2; m >= 1; m >>= 1) v += __shfl_xor_sync(kAll, v, m);
-  return v;
-}
-
-__device__ __forceinline__ long long globaltimer() {
-  long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ float bclip(float v, float b) { return v > b ? b : (v < -b ? -b : v); }
-
-// Forces of up to 4 rows named by lanes [k, k+4) of the group (ids < 0: none),
-// all groups of the warp in step (the caller keeps the warp converged).  xi is the
-// row's FP32 master value.  In the BF16 form the rows are read as BF16; a pair
-// whose squared distance from those reads is below a.near_r is read again from
-// the FP32 master and recomputed, so that the rounding of the copy does not bias
-// close pairs (their distance is then comparable with the BF16 rounding step).
-template <int D, int VPW, bool kBF16, bool kAttract>
-__device__ __forceinline__ void group_forces(const BatchedArgs &a, Row<D, VPW> &acc, const Row<D, VPW> &xi,
-                                             int64_t voff, int ids, int k, int gbase, int gl, float lr,
-                                             float &loss) {
-  constexpr int L = Row<D, VPW>::L, P = Row<D, VPW>::P;
-  constexpr int U = L >= 4 ? 4 : L;
-  Row<D, VPW> xn[U];
-  int nid[U];
-  float r[U];
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    int n = __shfl_sync(kAll, ids, gbase + k + u);
-    nid[u] = n;
-    if (n >= 0) load_row<D, VPW, kBF16>(xn[u], a, voff + n, gl);
-    else xn[u] = xi;
-  }
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    float p = 0.f;
-#pragma unroll
-    for (int t = 0; t < P; ++t) {
-      const float d = xi.v[t] - xn[u].v[t];
-      p = fmaf(d, d, p);
-    }
-    r[u] = group_sum<L>(p);
-  }
-  if constexpr (kBF16) {
-    bool near[U], any = false;
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      near[u] = nid[u] >= 0 && r[u] < a.near_r;
-      any |= near[u];
-    }
-    if (__any_sync(kAll, any)) {
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (near[u]) load_row<D, VPW, false>(xn[u], a, voff + nid[u], gl);
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        float p = 0.f;
-#pragma unroll
-        for (int t = 0; t < P; ++t) {
-          const float d = xi.v[t] - xn[u].v[t];
-          p = fmaf(d, d, p);
-        }
-        p = group_sum<L>(p);
-        if (near[u]) r[u] = p;
-      }
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    float c = kAttract ? -2.0f / (1.0f + r[u]) : 2.0f / ((r[u] + 1e-6f) * (1.0f + r[u]));
-    if (nid[u] < 0) c = 0.f;
-#pragma unroll
-    for (int t = 0; t < P; ++t) acc.v[t] = fmaf(lr, bclip((xi.v[t] - xn[u].v[t]) * c, a.bound), acc.v[t]);
-    if (nid[u] >= 0 && gl == 0) loss += kAttract ? log1pf(r[u]) : logf((1.0f + r[u]) / (r[u] + 1e-6f));
-  }
-}
-
-// x[row0 + i] += stage[i] for i < count (and the BF16 copy), every thread's
-// loads issued before its stores.
-template <bool kBF16>
-__device__ __forceinline__ void update_rows(float *xm, __nv_bfloat16 *xb, const float *stage, int64_t row0, int count,
-                                            int tid, int nthreads) {
-  constexpr int K = 4;
-  for (int b0 = tid * 4; b0 < count; b0 += nthreads * 4 * K) {
-    float4 m[K], st[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int idx = b0 + k * nthreads * 4;
-      if (idx < count) {
-        m[k] = __ldcg(reinterpret_cast<const float4 *>(xm + row0 + idx));
-        st[k] = __ldcg(reinterpret_cast<const float4 *>(stage + idx));
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int idx = b0 + k * nthreads * 4;
-      if (idx < count) {
-        m[k].x += st[k].x;
-        m[k].y += st[k].y;
-        m[k].z += st[k].z;
-        m[k].w += st[k].w;
-        *reinterpret_cast<float4 *>(xm + row0 + idx) = m[k];
-        if constexpr (kBF16) {
-          __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(xb + row0 + idx);
-          o[0] = __floats2bfloat162_rn(m[k].x, m[k].y);
-          o[1] = __floats2bfloat162_rn(m[k].z, m[k].w);
-        }
-      }
-    }
-  }
-}
-
-// Split rows of a minibatch: the pieces of each row summed in piece order.
-template <int D>
-__device__ __forceinline__ void combine_split_rows(const BatchedArgs &a, const float *slots, float *stage, int s0, int s1,
-                                                   int warp, int nwarps, int lane) {
-  for (int i = s0 + warp; i < s1; i += nwarps) {
-    const SplitRow sr = a.splits[i];
-    dev::Frag<D> acc;
-    dev::sum_slots<D>(acc, slots + size_t(sr.first_slot) * D, sr.nparts, lane);
-    dev::store<D, false>(acc, stage + size_t(sr.row) * D, lane);
-  }
-}
-
-template <int D, int VPW, int WARPS, bool kBF16>
-__global__ void __launch_bounds__(WARPS * 32) batched_kernel(const BatchedArgs a) {
-  constexpr int L = Row<D, VPW>::L, P = Row<D, VPW>::P;
-  static_assert(P % 2 == 0, "components per lane must be even");
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int grp = lane / L, gl = lane % L, gbase = grp * L;
-  __shared__ int sh_graph;
-  __shared__ double sh_loss[WARPS];
-  float *stage = a.stage + size_t(blockIdx.x) * a.batch * D;
-  float *slots = a.slots + size_t(blockIdx.x) * a.slot_stride * D;
-  const int skip_last = a.quirks;
-
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int i = atomicAdd(a.next_graph, 1);
-      sh_graph = i < a.n_graphs ? a.order[i] : -1;
-    }
-    __syncthreads();
-    const int g = sh_graph;
-    __syncthreads();
-    if (g < 0) return;
-    if (a.trace && threadIdx.x == 0) {
-      a.trace[3 * g] = globaltimer();
-      a.trace[3 * g + 2] = blockIdx.x;
-    }
-    const GraphInfo G = a.graphs[g];
-    const int skip = skip_last ? G.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
-    for (int e = 0; e < a.epochs; ++e) {
-      const float lr = a.lr[e];
-      double wloss = 0.0;  // this warp's share of the epoch loss, in item order
-      for (int j = 0; j < G.batches; ++j) {
-        const int64_t bi = G.batch_off + j;
-        const int64_t it0 = a.batch_item_off[bi];
-        const int n_items = int(a.batch_item_off[bi + 1] - a.batch_item_off[bi]);
-        const int base = j * a.batch;
-        const int rows = min(a.batch, G.n - base);
-        const int rep_rows = (a.quirks && e > 0) ? G.last_batch_size : rows;  // algo.hpp:167-169, 594
-        const int32_t *negs = a.negs + G.neg_off + (size_t(e) * G.batches + j) * a.ns;
-        // ---- 1. items, VPW per warp at a time
-        for (int i0 = warp * VPW; i0 < n_items; i0 += WARPS * VPW) {
-          const int my = i0 + grp;
-          const bool has = my < n_items;
-          WorkItem it{};
-          if (has) it = a.items[it0 + my];
-          Row<D, VPW> xi, acc;
-#pragma unroll
-          for (int t = 0; t < P; ++t) acc.v[t] = 0.f;
-          if (has) load_row<D, VPW, false>(xi, a, G.voff + base + it.row, gl);
-          else
-#pragma unroll
-            for (int t = 0; t < P; ++t) xi.v[t] = 0.f;
-          float loss = 0.f;
-          const int cnt = has ? it.e_end - it.e_begin : 0;
-          int maxcnt = cnt;
-#pragma unroll
-          for (int m = 16; m >= L; m >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kAll, maxcnt, m));
-          for (int c0 = 0; c0 < maxcnt; c0 += L) {
-            int ids = -1;
-            if (gl < cnt - c0) {
-              ids = __ldg(a.col + G.eoff + it.e_begin + c0 + gl);
-              if (ids == skip) ids = -1;
-            }
-            for (int k = 0; k < L && c0 + k < maxcnt; k += (L >= 4 ? 4 : L))
-              group_forces<D, VPW, kBF16, true>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss);
-          }
-          const bool repulse = has && it.part == 0 && it.row < rep_rows;
-          const bool any_rep = __any_sync(kAll, repulse);
-          for (int k0 = 0; any_rep && k0 < a.ns; k0 += L) {
-            int ids = -1;
-            if (repulse && gl < a.ns - k0) {
-              ids = __ldg(negs + k0 + gl);
-              if (ids >= G.n) ids = -1;  // a draw equal to n contributes nothing
-            }
-            for (int k = 0; k < L && k0 + k < a.ns; k += (L >= 4 ? 4 : L))
-              group_forces<D, VPW, kBF16, false>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss);
-          }
-          if (has) {
-            float *dst = it.nparts > 1 ? slots + size_t(it.first_slot + it.part) * D : stage + size_t(it.row) * D;
-#pragma unroll
-            for (int t = 0; t < P; t += 2) *reinterpret_cast<float2 *>(dst + gl * P + t) = make_float2(acc.v[t], acc.v[t + 1]);
-          }
-          // item loss, fixed order: groups of the warp in order
-#pragma unroll
-          for (int q = 0; q < VPW; ++q) wloss += double(__shfl_sync(kAll, loss, q * L));
-        }
-        __syncthreads();
-        // ---- 2. split rows: pieces in piece order
-        combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], warp, WARPS, lane);
-        __syncthreads();
-        // ---- 3. update (algo.hpp:651-666)
-        update_rows<kBF16>(a.xm, a.xb, stage, (G.voff + base) * D, rows * D, threadIdx.x, WARPS * 32);
-        __syncthreads();
-      }
-      if (lane == 0) sh_loss[warp] = wloss;
-      __syncthreads();
-      if (threadIdx.x == 0 && a.compute_loss) {
-        double s = 0.0;
-        for (int w = 0; w < WARPS; ++w) s += sh_loss[w];
-        a.loss[size_t(g) * a.epochs + e] = s;
-      }
-      __syncthreads();
-    }
-    if (a.trace && threadIdx.x == 0) a.trace[3 * g + 1] = globaltimer();
-  }
-}
-
-
-// ---------------------------------------------------------------- staged kernel
-//
-// The same per-graph step with the rows a warp reads staged in shared memory by
-// 16-byte asynchronous copies (cp.async, through L2) instead of loaded into
-// registers, so the bytes in flight per SM are bounded by shared memory, not by
-// registers, and the copies of later chunks overlap the arithmetic of the current
-// one.  Every warp runs its own pipeline over its chunks (work items i = warp,
-// warp + W, ... of the minibatch; a chunk is at most cap <= 32 CSR entries):
-//   column ids of chunk k+S are loaded while the rows of chunk k+S-1 are copied
-//   (own row from the FP32 master, neighbours from the BF16 copy or the FP32
-//   master) into ring slot (k+S-1) mod S, and chunk k is computed from slot k mod S
-//   once its copy group has landed (cp.async.wait_group S-1).
-// Each warp also copies the minibatch's ns negatives into its own area (with its
-// first chunk).  A pair is computed by dim/8 lanes (8 components each),
-// 32/(dim/8) pairs per warp step and NS steps in flight.  Results go to the
-// team's staging rows as in the register kernel; the minibatch ends with the same
-// combine and update.  No wait spins: every wait is a hardware wait on this
-// thread's own copies or a CTA barrier.
-
-constexpr int kStagedMaxNs = 32;
-
-template <int D, bool kBF16>
-struct StagedLayout {
-  static constexpr int kRowB = kBF16 ? 2 * D : 4 * D;  // a neighbour row in shared memory
-  static constexpr int kXiB = 4 * D;                   // the chunk's own row (FP32 master)
-  __host__ __device__ static constexpr int slot_bytes(int cap) { return kXiB + cap * kRowB; }
-  // per warp: S slots, the negatives (ns rows), 32 work items
-  __host__ __device__ static size_t warp_bytes(int S, int cap, int ns) {
-    return size_t(S) * slot_bytes(cap) + size_t(ns) * kRowB + 32 * sizeof(WorkItem);
-  }
-  __host__ __device__ static size_t bytes(int W, int S, int cap, int ns) { return size_t(W) * warp_bytes(S, cap, ns); }
-};
-
-// Copies `rows` rows (ids: lane j holds row j's vertex, local to voff) of
-// kRowB bytes from `base` into consecutive rows at `dst`, 16 bytes per lane per
-// instruction.
-template <int kRowB>
-__device__ __forceinline__ void copy_rows(uint32_t dst, const unsigned char *base, int64_t voff, int id, int rows,
-                                          int lane) {
-  constexpr int PR = kRowB / 16;  // pieces per row
-  const int total = rows * PR;
-  for (int p0 = 0; p0 < total; p0 += 32) {
-    const int p = p0 + lane;
-    const int row = p / PR;
-    const int rid = __shfl_sync(kAll, id, row & 31);
-    if (p < total) dev::cp_async16(dst + row * kRowB + (p % PR) * 16, base + (voff + rid) * kRowB + (p % PR) * 16);
-  }
-}
-
-// Pair layout of the staged kernel: a pair is computed by LP = dim/8 lanes, each
-// holding 8 components (16 bytes of a BF16 row), so one warp step covers
-// G = 32/LP pairs: lane l works on pair l / LP of the step, components
-// [8 (l % LP), 8 (l % LP) + 8).  A row's pairs are spread over the G groups and
-// the groups' accumulators are summed (fixed order) when the row is done.
-template <int D>
-struct PairLanes {
-  static constexpr int LP = D / 8;
-  static constexpr int G = 32 / LP;
-};
-
-// 8 components of a row in shared memory (BF16 or FP32) for lane-in-pair gl.
-template <bool kBF16>
-__device__ __forceinline__ void ld8(float (&v)[8], const unsigned char *row, int gl) {
-  if constexpr (kBF16) {
-    const uint4 u = *reinterpret_cast<const uint4 *>(row + gl * 16);
-    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      v[2 * i] = __uint_as_float(w[i] << 16);
-      v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-    }
-  } else {
-    const float4 x = *reinterpret_cast<const float4 *>(row + gl * 32);
-    const float4 y = *reinterpret_cast<const float4 *>(row + gl * 32 + 16);
-    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
-    v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
-  }
-}
-
-// NS warp steps of pairs (xi, rows[kb .. kb + NS*G)), rows past `count` skipped;
-// valid bit k of vmask: pair k counts (rows of pairs that do not count hold real
-// data, so they only need c = 0).
-//
-// Clip: |c * diff_k| <= |c| sqrt(r) for every component k, so when
-// c^2 r <= bound^2 no component reaches the bound and the clip of
-// algo.hpp:643 is the identity.  That always holds for the attractive force at
-// bound >= 1 (|c| sqrt(r) = 2 sqrt(r) / (1 + r) <= 1) and for repulsion at
-// r >= 0.25; a step in which some pair may clip takes the clipped path.
-//
-// BF16 form: a pair whose distance from the BF16 rows is below a.near_r is
-// recomputed from the FP32 master row (global id: lane k of `ids`).
-template <int D, int NS, bool kBF16, bool kAttract>
-__device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8], const float (&xi)[8],
-                                           const unsigned char *rows, int row_bytes, int kb, int count, unsigned vmask,
-                                           int ids, int64_t voff, float lr, float &loss, int lane) {
-  constexpr int LP = PairLanes<D>::LP, G = PairLanes<D>::G;
-  const int q = lane / LP, gl = lane % LP;
-  float d[NS][8], r[NS];
-  int k[NS];
-  bool ok[NS];
-#pragma unroll
-  for (int st = 0; st < NS; ++st) {
-    k[st] = kb + st * G + q;
-    float xn[8];
-    if (k[st] < count) {
-      ld8<kBF16>(xn, rows + k[st] * row_bytes, gl);
-    } else {
-#pragma unroll
-      for (int t = 0; t < 8; ++t) xn[t] = xi[t];
-    }
-    float p = 0.f;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      d[st][t] = xi[t] - xn[t];
-      p = fmaf(d[st][t], d[st][t], p);
-    }
-    r[st] = p;
-    ok[st] = k[st] < count && ((vmask >> k[st]) & 1u);
-  }
-#pragma unroll
-  for (int m = LP / 2; m >= 1; m >>= 1)
-#pragma unroll
-    for (int st = 0; st < NS; ++st) r[st] += __shfl_xor_sync(kAll, r[st], m);
-  if constexpr (kBF16) {
-    bool near[NS], any = false;
-#pragma unroll
-    for (int st = 0; st < NS; ++st) {
-      near[st] = ok[st] && r[st] < a.near_r;
-      any |= near[st];
-    }
-    if (__any_sync(kAll, any)) {
-#pragma unroll
-      for (int st = 0; st < NS; ++st) {
-        const int gid = __shfl_sync(kAll, ids, k[st] & 31);
-        float p = 0.f;
-        if (near[st]) {
-          const float4 *src = reinterpret_cast<const float4 *>(a.xm + (voff + gid) * D + gl * 8);
-          const float4 x = __ldcg(src), y = __ldcg(src + 1);
-          const float f[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            d[st][t] = xi[t] - f[t];
-            p = fmaf(d[st][t], d[st][t], p);
-          }
-        }
-#pragma unroll
-        for (int m = LP / 2; m >= 1; m >>= 1) p += __shfl_xor_sync(kAll, p, m);
-        if (near[st]) r[st] = p;
-      }
-    }
-  }
-  float c[NS];
-  bool may_clip = false;
-#pragma unroll
-  for (int st = 0; st < NS; ++st) {
-    c[st] = kAttract ? __fdividef(-2.0f, 1.0f + r[st]) : __fdividef(2.0f, (r[st] + 1e-6f) * (1.0f + r[st]));
-    if (!ok[st]) c[st] = 0.f;
-    if (ok[st] && gl == 0) loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
-    may_clip |= c[st] * c[st] * r[st] > 0.98f * a.bound * a.bound;
-  }
-  if (!__any_sync(kAll, may_clip)) {
-#pragma unroll
-    for (int st = 0; st < NS; ++st) {
-      const float lc = lr * c[st];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc[t] = fmaf(lc, d[st][t], acc[t]);
-    }
-  } else {
-#pragma unroll
-    for (int st = 0; st < NS; ++st)
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc[t] = fmaf(lr, bclip(d[st][t] * c[st], a.bound), acc[t]);
-  }
-}
-
-// All pairs of xi with rows [0, count).
-template <int D, int NS, bool kBF16, bool kAttract>
-__device__ __forceinline__ void staged_pairs(const BatchedArgs &a, float (&acc)[8], const float (&xi)[8],
-                                             const unsigned char *rows, int row_bytes, int count, unsigned vmask,
-                                             int ids, int64_t voff, float lr, float &loss, int lane) {
-  constexpr int G = PairLanes<D>::G;
-  int kb = 0;
-  for (; kb + NS * G <= count; kb += NS * G)
-    pair_steps<D, NS, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
-  if constexpr (NS > 1) {
-    for (; kb < count; kb += G)
-      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
-  } else {
-    if (kb < count)
-      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
-  }
-}
-
-
-template <int D, int NS, int S, bool kBF16>
-__global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
-  using Lay = StagedLayout<D, kBF16>;
-  constexpr int kRowB = Lay::kRowB, kXiB = Lay::kXiB;
-  constexpr int LP = PairLanes<D>::LP;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int W = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gl = lane % LP;
-  const int cap = a.cap, slotB = Lay::slot_bytes(cap);
-  unsigned char *ring = smem + size_t(warp) * Lay::warp_bytes(S, cap, a.ns);
-  unsigned char *negrows = ring + size_t(S) * slotB;
-  WorkItem *my_items = reinterpret_cast<WorkItem *>(negrows + size_t(a.ns) * kRowB);
-  const uint32_t ring_s = dev::smem_u32(ring), neg_s = dev::smem_u32(negrows);
-  __shared__ int sh_graph;
-  __shared__ double sh_loss[16];
-  float *stage = a.stage + size_t(blockIdx.x) * a.batch * D;
-  float *slots = a.slots + size_t(blockIdx.x) * a.slot_stride * D;
-  const unsigned char *src = kBF16 ? reinterpret_cast<const unsigned char *>(a.xb)
-                                   : reinterpret_cast<const unsigned char *>(a.xm);
-  const unsigned char *srcm = reinterpret_cast<const unsigned char *>(a.xm);
-
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int i = atomicAdd(a.next_graph, 1);
-      sh_graph = i < a.n_graphs ? a.order[i] : -1;
-    }
-    __syncthreads();
-    const int g = sh_graph;
-    __syncthreads();
-    if (g < 0) break;
-    if (a.trace && threadIdx.x == 0) {
-      a.trace[3 * g] = globaltimer();
-      a.trace[3 * g + 2] = blockIdx.x;
-    }
-    const GraphInfo G = a.graphs[g];
-    const int skip = a.quirks ? G.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
-    for (int e = 0; e < a.epochs; ++e) {
-      const float lr = a.lr[e];
-      double wloss = 0.0;
-      for (int j = 0; j < G.batches; ++j) {
-        const int64_t bi = G.batch_off + j;
-        const int64_t it0 = a.batch_item_off[bi];
-        const int n_items = int(a.batch_item_off[bi + 1] - it0);
-        const int base = j * a.batch;
-        const int rows = min(a.batch, G.n - base);
-        const int rep_rows = (a.quirks && e > 0) ? G.last_batch_size : rows;  // algo.hpp:167-169, 594
-        const int32_t *negs = a.negs + G.neg_off + (size_t(e) * G.batches + j) * a.ns;
-        // this minibatch's negatives: lane k holds draw k; a draw equal to n
-        // contributes nothing (its slot copies row 0 so that it holds real data)
-        const int nraw = lane < a.ns ? __ldg(negs + lane) : -1;
-        const int nid = nraw < G.n ? nraw : 0;
-        const unsigned neg_valid = __ballot_sync(kAll, lane < a.ns && nraw < G.n);
-        const int nmine = n_items > warp ? (n_items - warp + W - 1) / W : 0;
-        for (int r0 = 0; r0 < nmine; r0 += 32) {
-          const int nr = min(32, nmine - r0);
-          if (lane < nr) my_items[lane] = a.items[it0 + warp + int64_t(r0 + lane) * W];
-          __syncwarp();
-          // lane l: column id of CSR entry l of chunk k (-1 past its end)
-          auto load_cols = [&](int k) -> int {
-            const WorkItem &it = my_items[k];
-            return lane < it.e_end - it.e_begin ? __ldg(a.col + G.eoff + it.e_begin + lane) : -1;
-          };
-          int issued = 0;  // chunks of this round whose copies were committed
-          auto issue = [&](int k, int id) {
-            const uint32_t slot = ring_s + uint32_t((k % S) * slotB);
-            const int cnt = __popc(__ballot_sync(kAll, id >= 0));
-            const int64_t own = G.voff + base + my_items[k].row;
-            for (int p = lane; p < kXiB / 16; p += 32) dev::cp_async16(slot + p * 16, srcm + own * kXiB + p * 16);
-            copy_rows<kRowB>(slot + kXiB, src, G.voff, id, cnt, lane);
-            if (k == 0 && r0 == 0) copy_rows<kRowB>(neg_s, src, G.voff, nid, a.ns, lane);
-            dev::cp_async_commit();
-            ++issued;
-          };
-          int idq[S - 1];
-#pragma unroll
-          for (int i = 0; i < S - 1; ++i) idq[i] = i < nr ? load_cols(i) : -1;
-#pragma unroll
-          for (int i = 0; i < S - 1; ++i) {
-            if (i < nr) issue(i, idq[i]);
-            else dev::cp_async_commit();
-          }
-          int next = S - 1 < nr ? load_cols(S - 1) : -1;
-          for (int k = 0; k < nr; ++k) {
-            int nxt = -1;
-            if (k + S - 1 < nr) {
-              issue(k + S - 1, next);
-              nxt = next;
-            } else {
-              dev::cp_async_commit();  // an empty group keeps "S-1 groups after chunk k"
-            }
-            next = k + S < nr ? load_cols(k + S) : -1;
-            const int ids = idq[0];
-#pragma unroll
-            for (int i = 0; i + 1 < S - 1; ++i) idq[i] = idq[i + 1];
-            idq[S - 2] = nxt;
-            // ---- chunk k: its group is the oldest of the S in flight
-            dev::cp_async_wait<S - 1>();
-            __syncwarp();
-            const WorkItem it = my_items[k];
-            const unsigned char *slot = ring + size_t(k % S) * slotB;
-            float xi[8], acc[8];
-            ld8<false>(xi, slot, gl);
-#pragma unroll
-            for (int t = 0; t < 8; ++t) acc[t] = 0.f;
-            float loss = 0.f;
-            const int cnt = it.e_end - it.e_begin;
-            const unsigned vmask = __ballot_sync(kAll, ids >= 0 && ids != skip);
-            staged_pairs<D, NS, kBF16, true>(a, acc, xi, slot + kXiB, kRowB, cnt, vmask, ids, G.voff, lr, loss, lane);
-            if (it.part == 0 && it.row < rep_rows && a.ns > 0)
-              staged_pairs<D, NS, kBF16, false>(a, acc, xi, negrows, kRowB, a.ns, neg_valid, nid, G.voff, lr, loss,
-                                                lane);
-            // the groups' accumulators, summed; lanes of group 0 store the row
-#pragma unroll
-            for (int m = 16; m >= LP; m >>= 1)
-#pragma unroll
-              for (int t = 0; t < 8; ++t) acc[t] += __shfl_xor_sync(kAll, acc[t], m);
-            float *dst = it.nparts > 1 ? slots + size_t(it.first_slot + it.part) * D : stage + size_t(it.row) * D;
-            if (lane < LP) {
-              reinterpret_cast<float4 *>(dst + gl * 8)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-              reinterpret_cast<float4 *>(dst + gl * 8)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
-            }
-#pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kAll, loss, m);
-            wloss += double(loss);
-            __syncwarp();
-          }
-        }
-        dev::cp_async_wait<0>();
-        __syncthreads();
-        combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], warp, W, lane);
-        __syncthreads();
-        update_rows<kBF16>(a.xm, a.xb, stage, (G.voff + base) * D, rows * D, threadIdx.x, blockDim.x);  // algo.hpp:651-666
-        __syncthreads();
-      }
-      if (lane == 0) sh_loss[warp] = wloss;
-      __syncthreads();
-      if (threadIdx.x == 0 && a.compute_loss) {
-        double t = 0.0;
-        for (int w = 0; w < W; ++w) t += sh_loss[w];
-        a.loss[size_t(g) * a.epochs + e] = t;
-      }
-      __syncthreads();
-    }
-    if (a.trace && threadIdx.x == 0) a.trace[3 * g + 1] = globaltimer();
-  }
-}
-
-// ---------------------------------------------------------------- dispatch
-
-typedef void (*BatchedKernel)(BatchedArgs);
-
-// A team shape exists when every lane of a group holds an even number of components.
-template <int D, int V>
-constexpr bool kShapeOk = (D / (32 / V)) % 2 == 0;
-
-template <int D, bool kBF16, int V>
-BatchedKernel pick_warps(int warps) {
-  if constexpr (kShapeOk<D, V>) {
-    switch (warps) {
-      case 4: return batched_kernel<D, V, 4, kBF16>;
-      case 8: return batched_kernel<D, V, 8, kBF16>;
-      case 16: return batched_kernel<D, V, 16, kBF16>;
-      case 32: return batched_kernel<D, V, 32, kBF16>;
-    }
-  }
-  return nullptr;
-}
-
-template <int D, bool kBF16>
-BatchedKernel pick(int vpw, int warps) {
-  switch (vpw) {
-    case 1: return pick_warps<D, kBF16, 1>(warps);
-    case 2: return pick_warps<D, kBF16, 2>(warps);
-    case 4: return pick_warps<D, kBF16, 4>(warps);
-  }
-  return nullptr;
-}
-
-BatchedKernel pick_register(int dim, bool bf16, int vpw, int warps) {
-  switch (dim) {
-    case 32: return bf16 ? pick<32, true>(vpw, warps) : pick<32, false>(vpw, warps);
-    case 64: return bf16 ? pick<64, true>(vpw, warps) : pick<64, false>(vpw, warps);
-    case 128: return bf16 ? pick<128, true>(vpw, warps) : pick<128, false>(vpw, warps);
-  }
-  return nullptr;
-}
-
-template <int D, bool kBF16>
-BatchedKernel pick_staged_fn(int steps, int stages) {
-  if (steps == 1 && stages == 3) return staged_kernel<D, 1, 3, kBF16>;
-  if (steps == 1 && stages == 4) return staged_kernel<D, 1, 4, kBF16>;
-  if (steps == 2 && stages == 3) return staged_kernel<D, 2, 3, kBF16>;
-  if (steps == 2 && stages == 4) return staged_kernel<D, 2, 4, kBF16>;
-  return nullptr;
-}
 
 // Largest dynamic shared memory a staged team may use (the static part is small).
 constexpr size_t kStagedSmemMax = 227 * 1024 - 1024;
@@ -740,6 +38,11 @@ constexpr size_t kStagedSmemMax = 227 * 1024 - 1024;
 template <int D, bool kBF16>
 size_t staged_smem(const de_batch_shape &s, int ns) {
   return StagedLayout<D, kBF16>::bytes(s.team_warps, s.stages, s.edge_cap, ns);
+}
+
+template <int D, bool kBF16>
+size_t rows_smem(const de_batch_shape &s, int ns) {
+  return RowsLayout<D, kBF16>::bytes(s.team_warps, s.stages, s.edge_cap, ns);
 }
 
 // The kernel, its block size and dynamic shared memory for a team shape; fn is
@@ -758,19 +61,39 @@ KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) 
     k.block = 32 * s.team_warps;
     return k;
   }
-  if (s.kernel != DE_BATCH_STAGED || s.team_warps < 2 || s.team_warps > 16 || s.edge_cap < 1 || s.edge_cap > 32)
+  if ((s.kernel != DE_BATCH_STAGED && s.kernel != DE_BATCH_ROWS) || s.team_warps < 2 || s.team_warps > 16 ||
+      s.edge_cap < 1 || s.edge_cap > 32)
     return k;
+  if (s.kernel == DE_BATCH_ROWS) {
+    switch (dim) {
+      case 32:
+        k.fn = pick_rows(32, bf16, s.pairs, s.stages);
+        k.smem = bf16 ? rows_smem<32, true>(s, ns) : rows_smem<32, false>(s, ns);
+        break;
+      case 64:
+        k.fn = pick_rows(64, bf16, s.pairs, s.stages);
+        k.smem = bf16 ? rows_smem<64, true>(s, ns) : rows_smem<64, false>(s, ns);
+        break;
+      case 128:
+        k.fn = pick_rows(128, bf16, s.pairs, s.stages);
+        k.smem = bf16 ? rows_smem<128, true>(s, ns) : rows_smem<128, false>(s, ns);
+        break;
+    }
+    if (k.smem > kStagedSmemMax) k.fn = nullptr;
+    k.block = 32 * s.team_warps;
+    return k;
+  }
   switch (dim) {
     case 32:
-      k.fn = bf16 ? pick_staged_fn<32, true>(s.pairs, s.stages) : pick_staged_fn<32, false>(s.pairs, s.stages);
+      k.fn = pick_staged(32, bf16, s.pairs, s.stages);
       k.smem = bf16 ? staged_smem<32, true>(s, ns) : staged_smem<32, false>(s, ns);
       break;
     case 64:
-      k.fn = bf16 ? pick_staged_fn<64, true>(s.pairs, s.stages) : pick_staged_fn<64, false>(s.pairs, s.stages);
+      k.fn = pick_staged(64, bf16, s.pairs, s.stages);
       k.smem = bf16 ? staged_smem<64, true>(s, ns) : staged_smem<64, false>(s, ns);
       break;
     case 128:
-      k.fn = bf16 ? pick_staged_fn<128, true>(s.pairs, s.stages) : pick_staged_fn<128, false>(s.pairs, s.stages);
+      k.fn = pick_staged(128, bf16, s.pairs, s.stages);
       k.smem = bf16 ? staged_smem<128, true>(s, ns) : staged_smem<128, false>(s, ns);
       break;
   }
@@ -947,7 +270,7 @@ int teams_for(de_batch *b, const KernelPick &k) {
 // here may run inside a stream capture: it allocates and copies synchronously.
 int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, const de_batch_shape &shape) {
   BCUDA(b, cudaSetDevice(b->device));
-  if (shape.kernel == DE_BATCH_STAGED && ns > kStagedMaxNs)
+  if (shape.kernel != DE_BATCH_REGISTER && ns > kStagedMaxNs)
     return bfail(b, DE_ERR_UNSUPPORTED, "the staged kernel takes at most 32 negatives per minibatch");
   const KernelPick k = pick_kernel(b->dim, b->opt.precision == DE_PRECISION_BF16, shape, ns);
   if (!k.fn) return bfail(b, DE_ERR_UNSUPPORTED, "no kernel for this dim and team shape (or its shared memory is too large)");
@@ -1284,10 +607,11 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
     for (int w : {4, 8, 16, 32})
       for (int c : {32, 64, 128}) cand.push_back(de_batch_shape{DE_BATCH_REGISTER, v, w, c, 0, 0});
   if (ns <= kStagedMaxNs)
-    for (int w : {4, 8, 12, 16})
-      for (int c : {8, 16, 32})
-        for (int u : {1, 2})
-          for (int st : {3, 4}) cand.push_back(de_batch_shape{DE_BATCH_STAGED, 0, w, c, u, st});
+    for (int fam : {DE_BATCH_STAGED, DE_BATCH_ROWS})
+      for (int w : {4, 8, 12, 16})
+        for (int c : {8, 16, 32})
+          for (int u : {1, 2})
+            for (int st : {3, 4}) cand.push_back(de_batch_shape{fam, 0, w, c, u, st});
   const bool bf16 = b->opt.precision == DE_PRECISION_BF16;
   std::vector<double> lrs(epochs, lr);
   float best_ms = -1.f;

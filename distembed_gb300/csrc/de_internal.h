@@ -168,7 +168,8 @@ cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
 constexpr int kPlainWarps = 4;      // warps per CTA of the plain batch kernel
-constexpr int kPlainMinBlocks = 6;  // resident CTAs per SM the register budget targets
+constexpr int kPlainMinBlocks = 8;  // resident CTAs per SM the register budget targets (one wave of
+                                    // work items at minibatch 4096: 152 x 8 x 4 warps)
 constexpr int kMaxEdgeCap = 32;     // CSR entries per work item: one per lane
 
 }  // namespace de

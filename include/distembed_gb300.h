@@ -172,9 +172,13 @@ int de_batch_get_embeddings_f32(de_batch *b, int32_t graph, float *x);
  *                      (one chunk); pairs = warp steps in flight (1 or 2);
  *                      stages 3 or 4 ring slots per warp; at most 32 negatives
  *                      per minibatch
+ *   DE_BATCH_ROWS      the staged pipeline with one work item per group of
+ *                      dim/8 lanes (32/(dim/8) items per warp chunk); same
+ *                      fields as DE_BATCH_STAGED
  * A shape that does not exist for the batch's dim returns DE_ERR_UNSUPPORTED. */
 #define DE_BATCH_REGISTER 0
 #define DE_BATCH_STAGED 1
+#define DE_BATCH_ROWS 2
 typedef struct de_batch_shape {
   int32_t kernel;            /* DE_BATCH_*                                   */
   int32_t vertices_per_warp; /* register kernel                              */

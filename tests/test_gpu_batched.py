@@ -60,6 +60,7 @@ def x_init(i, n, dim):
 
 REG = dict(kernel="register", vertices_per_warp=4, team_warps=8, edge_cap=32)
 STAGED = dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3)
+ROWS = dict(kernel="rows", team_warps=4, edge_cap=16, pairs=2, stages=3)
 
 
 def run_batch(graphs, dim, epochs, batch, ns, lr, precision="fp32", shape=None, ids=None):
@@ -73,12 +74,17 @@ def run_batch(graphs, dim, epochs, batch, ns, lr, precision="fp32", shape=None, 
         return [b.get_embeddings(j).astype(np.float64) for j in range(len(graphs))], loss
 
 
-@pytest.mark.parametrize("kernel", ["register", "staged"])
+@pytest.mark.parametrize("kernel", ["register", "staged", "rows"])
 @pytest.mark.parametrize("dim", [32, 64, 128])
 def test_fp32_batch_matches_oracle_per_graph(dim, kernel):
     E, B, ns = 3, 256, 5
     lr = [0.02 * (1 - e / E) for e in range(E)]
-    shape = REG if kernel == "register" else (STAGED if dim < 128 else dict(STAGED, team_warps=4, edge_cap=16))
+    if kernel == "register":
+        shape = REG
+    elif kernel == "staged":
+        shape = STAGED if dim < 128 else dict(STAGED, team_warps=4, edge_cap=16)
+    else:
+        shape = ROWS if dim < 128 else dict(ROWS, team_warps=2, edge_cap=16)
     xs, loss = run_batch(GRAPHS, dim, E, B, ns, lr, shape=shape)
     for i, (kind, n, rp, c) in enumerate(GRAPHS):
         xo, lo = oracle.run(rp, c, x_init(i, n, dim), E, B, ns, lr, quirks=True)
@@ -95,7 +101,11 @@ SHAPES = [dict(kernel="register", vertices_per_warp=1, team_warps=4, edge_cap=32
           dict(kernel="staged", team_warps=16, edge_cap=8, pairs=2, stages=3),
           dict(kernel="staged", team_warps=8, edge_cap=16, pairs=2, stages=4),
           dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3),
-          dict(kernel="staged", team_warps=2, edge_cap=1, pairs=1, stages=4)]
+          dict(kernel="staged", team_warps=2, edge_cap=1, pairs=1, stages=4),
+          dict(kernel="rows", team_warps=4, edge_cap=16, pairs=1, stages=3),
+          dict(kernel="rows", team_warps=4, edge_cap=8, pairs=2, stages=4),
+          dict(kernel="rows", team_warps=2, edge_cap=32, pairs=2, stages=3),
+          dict(kernel="rows", team_warps=3, edge_cap=1, pairs=1, stages=4)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "-".join(str(v) for v in s.values()))
@@ -108,7 +118,7 @@ def test_every_team_shape_matches_oracle(shape):
         assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (shape, i)
 
 
-@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
+@pytest.mark.parametrize("shape", [REG, STAGED, ROWS], ids=["register", "staged", "rows"])
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
 def test_alone_equals_mix_bitwise(precision, shape):
     dim, E, B, ns = 64, 3, 256, 5
@@ -125,7 +135,7 @@ def test_alone_equals_mix_bitwise(precision, shape):
         assert np.array_equal(xp[j], xs[i]) and np.array_equal(lp[j], loss[i]), i
 
 
-@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
+@pytest.mark.parametrize("shape", [REG, STAGED, ROWS], ids=["register", "staged", "rows"])
 def test_bf16_batch_loss_within_one_percent(shape):
     dim, E, B, ns = 64, 4, 256, 5
     _, loss = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=shape)
@@ -147,7 +157,7 @@ def test_autotune_keeps_embeddings_and_picks_a_valid_shape():
             b.set_embeddings(i, x_init(i, n, dim))
         best, tried = b.autotune(1, B, ns, 0.02)
         assert len(tried) >= 36 and all(ms > 0 for _, ms in tried)
-        assert {sh["kernel"] for sh, _ in tried} == {0, 1}
+        assert {sh["kernel"] for sh, _ in tried} == {0, 1, 2}
         assert best == min(tried, key=lambda t: t[1])[0] == b.shape()
         for i, (_, n, _, _) in enumerate(graphs):
             assert np.array_equal(b.get_embeddings(i).astype(np.float64), x_init(i, n, dim))
@@ -216,13 +226,13 @@ def test_staged_rejects_more_than_32_negatives():
         assert ei.value.code == de.DE_ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("shape", [REG, STAGED], ids=["register", "staged"])
+@pytest.mark.parametrize("shape", [REG, STAGED, ROWS], ids=["register", "staged", "rows"])
 def test_hub_rows_and_many_chunks_per_warp(shape):
     # one graph whose minibatches hold far more than 32 chunks per warp (hub rows
     # split into cap-sized pieces), so the staged pipeline restarts within a minibatch
     n, rp, c = gg.rmat_csr(11, 32, seed=9)
     g = [("rmat", n, rp, c)]
-    sh = dict(shape, edge_cap=4, team_warps=2) if shape["kernel"] == "staged" else dict(shape, edge_cap=4)
+    sh = dict(shape, edge_cap=4, team_warps=2) if shape["kernel"] != "register" else dict(shape, edge_cap=4)
     xs, loss = run_batch(g, 32, 2, 512, 6, 0.02, shape=sh, ids=[50])
     xo, lo = oracle.run(rp, c, x_init(50, n, 32), 2, 512, 6, 0.02, quirks=True)
     assert rel_l2(xs[0], xo) <= RUN_REL_L2
