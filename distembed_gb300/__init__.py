@@ -43,7 +43,8 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
 
 class BatchShape(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int32), ("vertices_per_warp", ctypes.c_int32), ("team_warps", ctypes.c_int32),
-                ("edge_cap", ctypes.c_int32), ("pairs", ctypes.c_int32), ("stages", ctypes.c_int32)]
+                ("edge_cap", ctypes.c_int32), ("pairs", ctypes.c_int32), ("stages", ctypes.c_int32),
+                ("team_ctas", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -399,10 +400,11 @@ class Batch:
         self._check(lib().de_batch_get_embeddings_f32(self._h, g, out.ctypes.data))
         return out
 
-    def set_shape(self, kernel="register", vertices_per_warp=0, team_warps=8, edge_cap=32, pairs=0, stages=0):
+    def set_shape(self, kernel="register", vertices_per_warp=0, team_warps=8, edge_cap=32, pairs=0, stages=0,
+                  team_ctas=1):
         """Team shape (see de_batch_shape); kernel "register", "staged" or "rows" (or 0 / 1 / 2)."""
         k = BATCH_KERNEL.get(kernel, kernel)
-        sh = BatchShape(k, vertices_per_warp, team_warps, edge_cap, pairs, stages)
+        sh = BatchShape(k, vertices_per_warp, team_warps, edge_cap, pairs, stages, team_ctas)
         self._check(lib().de_batch_set_shape(self._h, ctypes.byref(sh)))
 
     def shape(self) -> dict:

@@ -51,10 +51,13 @@ struct KernelPick {
   BatchedKernel fn = nullptr;
   int block = 0;
   size_t smem = 0;
+  int ctas = 1;  // CTAs per cluster the kernel is launched with
 };
 
 KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) {
   KernelPick k;
+  if (s.team_ctas > 2 || (s.team_ctas == 2 && s.kernel != DE_BATCH_STAGED)) return k;
+  k.ctas = s.team_ctas == 2 ? 2 : 1;
   if (s.kernel == DE_BATCH_REGISTER) {
     if (s.edge_cap < 1 || s.edge_cap > 4096) return k;
     k.fn = pick_register(dim, bf16, s.vertices_per_warp, s.team_warps);
@@ -85,15 +88,15 @@ KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) 
   }
   switch (dim) {
     case 32:
-      k.fn = pick_staged(32, bf16, s.pairs, s.stages);
+      k.fn = pick_staged(32, bf16, s.pairs, s.stages, k.ctas);
       k.smem = bf16 ? staged_smem<32, true>(s, ns) : staged_smem<32, false>(s, ns);
       break;
     case 64:
-      k.fn = pick_staged(64, bf16, s.pairs, s.stages);
+      k.fn = pick_staged(64, bf16, s.pairs, s.stages, k.ctas);
       k.smem = bf16 ? staged_smem<64, true>(s, ns) : staged_smem<64, false>(s, ns);
       break;
     case 128:
-      k.fn = pick_staged(128, bf16, s.pairs, s.stages);
+      k.fn = pick_staged(128, bf16, s.pairs, s.stages, k.ctas);
       k.smem = bf16 ? staged_smem<128, true>(s, ns) : staged_smem<128, false>(s, ns);
       break;
   }
@@ -140,9 +143,14 @@ struct de_batch {
   size_t loss_cap = 0;
   float *d_stage = nullptr, *d_slots = nullptr;
   size_t stage_cap = 0, slots_cap = 0;
-  de_batch_shape shape{DE_BATCH_REGISTER, 4, 8, 32, 0, 0};
-  int teams = 0, block = 0;
+  de_batch_shape shape{DE_BATCH_REGISTER, 4, 8, 32, 0, 0, 1};
+  int teams = 0, block = 0, ctas = 1, n_big = 0;
   size_t smem = 0;
+  float *d_item_loss = nullptr;
+  size_t item_loss_cap = 0;
+  int32_t *d_cluster_slot = nullptr;
+  size_t cluster_slot_cap = 0;
+  int max_batch_items = 1;
   int32_t *d_err = nullptr;
   BatchedKernel kernel = nullptr;
   BatchedArgs args{};
@@ -186,6 +194,7 @@ int build_batched_schedule(de_batch *b, int B, int cap) {
   std::vector<SplitRow> splits;
   b->ginfo.assign(b->n_graphs, GraphInfo{});
   int max_slots = 1;
+  int64_t max_items = 1;
   int64_t batch_off = 0;
   for (int g = 0; g < b->n_graphs; ++g) {
     GraphInfo &G = b->ginfo[g];
@@ -221,6 +230,7 @@ int build_batched_schedule(de_batch *b, int B, int cap) {
       });
       max_slots = std::max(max_slots, slot);
       bitem.push_back(int64_t(items.size()));
+      max_items = std::max<int64_t>(max_items, bitem.back() - bitem[bitem.size() - 2]);
       bsplit.push_back(int32_t(splits.size()));
     }
     batch_off += G.batches;
@@ -228,6 +238,7 @@ int build_batched_schedule(de_batch *b, int B, int cap) {
   b->sched_batch = B;
   b->sched_cap = cap;
   b->max_slots = max_slots;
+  b->max_batch_items = int(max_items);
   // graphs largest first (LPT): by total work n + nnz
   b->order.resize(b->n_graphs);
   for (int g = 0; g < b->n_graphs; ++g) b->order[g] = g;
@@ -262,7 +273,25 @@ int teams_for(de_batch *b, const KernelPick &k) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.block, k.smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms < 1) sms = 1;
-  return std::min(per_sm * sms, b->n_graphs);
+  if (k.ctas == 1) return std::min(per_sm * sms, b->n_graphs);
+  // clusters of two CTAs: as many as can be resident at once (a cluster sits in one GPC)
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(2 * per_sm * sms);
+  cfg.blockDim = dim3(k.block);
+  cfg.dynamicSmemBytes = k.smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, k.fn, &cfg) != cudaSuccess || clusters < 1) {
+    cudaGetLastError();
+    clusters = std::max(1, per_sm * sms / 2);
+  }
+  return 2 * std::min(clusters, (b->n_graphs + 1) / 2);
 }
 
 // Everything of a run except the launch: schedule, negatives, rates, team staging
@@ -308,6 +337,26 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   const int teams = teams_for(b, k);
   if (int rc = bgrow(b, &b->d_stage, &b->stage_cap, size_t(teams) * B * b->dim)) return rc;
   if (int rc = bgrow(b, &b->d_slots, &b->slots_cap, size_t(teams) * b->max_slots * b->dim)) return rc;
+  if (int rc = bgrow(b, &b->d_item_loss, &b->item_loss_cap, size_t(teams) * b->max_batch_items)) return rc;
+  if (int rc = bgrow(b, &b->d_cluster_slot, &b->cluster_slot_cap, size_t(teams / 2 + 1))) return rc;
+  // graphs largest first by work (CSR entries, repulsive pairs and a fixed cost per
+  // minibatch, all per epoch); with two-CTA teams the graphs above 0.6 of the
+  // balanced share of one CTA are trained by a whole cluster
+  {
+    std::vector<double> w(b->n_graphs);
+    double total_w = 0;
+    for (int g = 0; g < b->n_graphs; ++g) {
+      w[g] = double(b->nnz[g]) + double(ns) * double(b->n[g]) + 900.0 * b->ginfo[g].batches;
+      total_w += w[g];
+    }
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return w[x] > w[y]; });
+    b->n_big = 0;
+    if (k.ctas == 2)
+      while (b->n_big < b->n_graphs && w[b->order[b->n_big]] > 0.6 * total_w / teams) ++b->n_big;
+    BCUDA(b, cudaMemcpyAsync(b->d_order, b->order.data(), b->order.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+  }
   BatchedArgs &a = b->args;
   a = BatchedArgs{};
   a.graphs = b->d_graphs;
@@ -337,6 +386,12 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   a.trace = b->d_trace;
   a.cap = cap;
   a.err = b->d_err;
+  a.n_big = b->n_big;
+  a.next_big = b->d_next + 1;
+  a.cluster_slot = b->d_cluster_slot;
+  a.item_loss = b->d_item_loss;
+  a.item_stride = b->max_batch_items;
+  b->ctas = k.ctas;
   b->kernel = k.fn;
   b->teams = teams;
   b->block = k.block;
@@ -346,8 +401,24 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
 
 // The whole run: reset the team work counter, then one persistent launch.
 int launch_batched(de_batch *b, cudaStream_t st) {
-  BCUDA(b, cudaMemsetAsync(b->d_next, 0, sizeof(int32_t), st));
-  b->kernel<<<b->teams, b->block, b->smem, st>>>(b->args);
+  BCUDA(b, cudaMemsetAsync(b->d_next, 0, 2 * sizeof(int32_t), st));
+  if (b->ctas == 1) {
+    b->kernel<<<b->teams, b->block, b->smem, st>>>(b->args);
+  } else {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(b->teams);
+    cfg.blockDim = dim3(b->block);
+    cfg.dynamicSmemBytes = b->smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    BCUDA(b, cudaLaunchKernelEx(&cfg, b->kernel, b->args));
+  }
   BCUDA(b, cudaGetLastError());
   return DE_OK;
 }
@@ -415,7 +486,7 @@ int de_batch_create(int32_t n_graphs, const int64_t *n, const int64_t *const *ro
   const size_t xn = size_t(b->total_n) * dim;
   if ((e = cudaMalloc(&b->d_col, std::max<size_t>(col32.size(), 1) * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_xm, xn * sizeof(float))) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_next, sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_next, 2 * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_trace, size_t(n_graphs) * 3 * sizeof(long long))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_err, sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMemsetAsync(b->d_err, 0, sizeof(int32_t), b->stream)) != cudaSuccess ||
@@ -445,7 +516,8 @@ int de_batch_destroy(de_batch *b) {
                   static_cast<void *>(b->d_bsplit), static_cast<void *>(b->d_splits), static_cast<void *>(b->d_negs),
                   static_cast<void *>(b->d_lr), static_cast<void *>(b->d_loss), static_cast<void *>(b->d_stage),
                   static_cast<void *>(b->d_slots), static_cast<void *>(b->d_trace),
-                  static_cast<void *>(b->d_err)})
+                  static_cast<void *>(b->d_err), static_cast<void *>(b->d_item_loss),
+                  static_cast<void *>(b->d_cluster_slot)})
     if (p) cudaFree(p);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -605,13 +677,17 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
   std::vector<de_batch_shape> cand;
   for (int v : {1, 2, 4})
     for (int w : {4, 8, 16, 32})
-      for (int c : {32, 64, 128}) cand.push_back(de_batch_shape{DE_BATCH_REGISTER, v, w, c, 0, 0});
+      for (int c : {32, 64, 128}) cand.push_back(de_batch_shape{DE_BATCH_REGISTER, v, w, c, 0, 0, 1});
   if (ns <= kStagedMaxNs)
     for (int fam : {DE_BATCH_STAGED, DE_BATCH_ROWS})
       for (int w : {4, 8, 12, 16})
         for (int c : {8, 16, 32})
           for (int u : {1, 2})
-            for (int st : {3, 4}) cand.push_back(de_batch_shape{fam, 0, w, c, u, st});
+            for (int st : {3, 4}) cand.push_back(de_batch_shape{fam, 0, w, c, u, st, 1});
+    for (int w : {8, 16})
+      for (int c : {16, 32})
+        for (int u : {1, 2})
+          for (int st : {3, 4}) cand.push_back(de_batch_shape{DE_BATCH_STAGED, 0, w, c, u, st, 2});
   const bool bf16 = b->opt.precision == DE_PRECISION_BF16;
   std::vector<double> lrs(epochs, lr);
   float best_ms = -1.f;

@@ -55,6 +55,14 @@ struct BatchedArgs {
   long long *trace;          // nullable: per graph {start ns, end ns, team}
   int32_t cap;               // staged kernel: CSR entries per chunk (<= 32)
   int32_t *err;              // staged kernel: set when a bounded wait gives up
+  // staged kernel with two-CTA teams: the first n_big graphs of `order` are trained
+  // by both CTAs of a cluster together (next_big counts them out), the rest by
+  // single CTAs (next_graph counts from order[n_big])
+  int32_t n_big;
+  int32_t *next_big;
+  int32_t *cluster_slot;     // [clusters] graph handed from CTA rank 0 to rank 1
+  float *item_loss;          // [teams, max items of a minibatch] loss of every work item
+  int32_t item_stride;
 };
 
 static __device__ __forceinline__ long long globaltimer() {
@@ -189,7 +197,7 @@ typedef void (*BatchedKernel)(BatchedArgs);
 
 // Kernel of each family for a dim, precision and shape; nullptr when none.
 BatchedKernel pick_register(int dim, bool bf16, int vpw, int warps);  // de_batched_reg.cu
-BatchedKernel pick_staged(int dim, bool bf16, int steps, int stages);  // de_batched_staged.cu
+BatchedKernel pick_staged(int dim, bool bf16, int steps, int stages, int ctas);  // de_batched_staged.cu
 BatchedKernel pick_rows(int dim, bool bf16, int steps, int stages);    // de_batched_rows.cu
 
 }  // namespace batched

@@ -138,7 +138,25 @@ __device__ __forceinline__ void staged_pairs(const BatchedArgs &a, float (&acc)[
 }
 
 
-template <int D, int NS, int S, bool kBF16>
+__device__ __forceinline__ int cluster_rank() {
+  int r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Both CTAs of the cluster: every thread arrives (release) and waits (acquire),
+// so each CTA's global writes before the barrier are visible to the other after it.
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// A team is one CTA or, with CT = 2, the two CTAs of a cluster working on one
+// graph: team warp tw = rank * W + warp of TW = nct * W, one shared staging area
+// (that of rank 0), barriers across both CTAs.  With CT = 2 a cluster first takes
+// the big graphs (order[0, n_big)) as one team; when they are gone its CTAs
+// take the remaining graphs one each.  The loss of an epoch is summed from the
+// per-item losses in item order, so it does not depend on the team's make-up.
+template <int D, int NS, int S, bool kBF16, int CT>
 __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
   using Lay = StagedLayout<D, kBF16>;
   constexpr int kRowB = Lay::kRowB, kXiB = Lay::kXiB;
@@ -152,23 +170,48 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
   WorkItem *my_items = reinterpret_cast<WorkItem *>(negrows + size_t(a.ns) * kRowB);
   const uint32_t ring_s = dev::smem_u32(ring), neg_s = dev::smem_u32(negrows);
   __shared__ int sh_graph;
-  __shared__ double sh_loss[16];
-  float *stage = a.stage + size_t(blockIdx.x) * a.batch * D;
-  float *slots = a.slots + size_t(blockIdx.x) * a.slot_stride * D;
   const unsigned char *src = kBF16 ? reinterpret_cast<const unsigned char *>(a.xb)
                                    : reinterpret_cast<const unsigned char *>(a.xm);
   const unsigned char *srcm = reinterpret_cast<const unsigned char *>(a.xm);
+  const int rank = CT == 2 ? cluster_rank() : 0;
+  bool coop = CT == 2;
 
   for (;;) {
-    if (threadIdx.x == 0) {
-      const int i = atomicAdd(a.next_graph, 1);
-      sh_graph = i < a.n_graphs ? a.order[i] : -1;
+    int g;
+    if (coop) {
+      if (threadIdx.x == 0 && rank == 0) {
+        const int i = atomicAdd(a.next_big, 1);
+        *reinterpret_cast<volatile int *>(a.cluster_slot + blockIdx.x / 2) = i < a.n_big ? a.order[i] : -1;
+        __threadfence();
+      }
+      cluster_sync();
+      g = __ldcg(a.cluster_slot + blockIdx.x / 2);
+      cluster_sync();  // rank 0 rewrites the slot only after both have read it
+      if (g < 0) {
+        coop = false;
+        continue;
+      }
+    } else {
+      if (threadIdx.x == 0) {
+        const int i = atomicAdd(a.next_graph, 1);
+        sh_graph = i < a.n_graphs - a.n_big ? a.order[a.n_big + i] : -1;
+      }
+      __syncthreads();
+      g = sh_graph;
+      __syncthreads();
+      if (g < 0) break;
     }
-    __syncthreads();
-    const int g = sh_graph;
-    __syncthreads();
-    if (g < 0) break;
-    if (a.trace && threadIdx.x == 0) {
+    const int nct = coop ? 2 : 1, trank = coop ? rank : 0;
+    const int tw = trank * W + warp, TW = nct * W;
+    const int team_blk = blockIdx.x - trank;
+    float *stage = a.stage + size_t(team_blk) * a.batch * D;
+    float *slots = a.slots + size_t(team_blk) * a.slot_stride * D;
+    float *item_loss = a.item_loss + size_t(team_blk) * a.item_stride;
+    auto team_sync = [&]() {
+      if (nct == 2) cluster_sync();
+      else __syncthreads();
+    };
+    if (a.trace && threadIdx.x == 0 && trank == 0) {
       a.trace[3 * g] = globaltimer();
       a.trace[3 * g + 2] = blockIdx.x;
     }
@@ -176,7 +219,7 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
     const int skip = a.quirks ? G.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
     for (int e = 0; e < a.epochs; ++e) {
       const float lr = a.lr[e];
-      double wloss = 0.0;
+      double eloss = 0.0;  // rank 0, thread 0: the epoch's loss, minibatch by minibatch
       for (int j = 0; j < G.batches; ++j) {
         const int64_t bi = G.batch_off + j;
         const int64_t it0 = a.batch_item_off[bi];
@@ -190,17 +233,16 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
         const int nraw = lane < a.ns ? __ldg(negs + lane) : -1;
         const int nid = nraw < G.n ? nraw : 0;
         const unsigned neg_valid = __ballot_sync(kAll, lane < a.ns && nraw < G.n);
-        const int nmine = n_items > warp ? (n_items - warp + W - 1) / W : 0;
+        const int nmine = n_items > tw ? (n_items - tw + TW - 1) / TW : 0;
         for (int r0 = 0; r0 < nmine; r0 += 32) {
           const int nr = min(32, nmine - r0);
-          if (lane < nr) my_items[lane] = a.items[it0 + warp + int64_t(r0 + lane) * W];
+          if (lane < nr) my_items[lane] = a.items[it0 + tw + int64_t(r0 + lane) * TW];
           __syncwarp();
           // lane l: column id of CSR entry l of chunk k (-1 past its end)
           auto load_cols = [&](int k) -> int {
             const WorkItem &it = my_items[k];
             return lane < it.e_end - it.e_begin ? __ldg(a.col + G.eoff + it.e_begin + lane) : -1;
           };
-          int issued = 0;  // chunks of this round whose copies were committed
           auto issue = [&](int k, int id) {
             const uint32_t slot = ring_s + uint32_t((k % S) * slotB);
             const int cnt = __popc(__ballot_sync(kAll, id >= 0));
@@ -209,7 +251,6 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
             copy_rows<kRowB>(slot + kXiB, src, G.voff, id, cnt, lane);
             if (k == 0 && r0 == 0) copy_rows<kRowB>(neg_s, src, G.voff, nid, a.ns, lane);
             dev::cp_async_commit();
-            ++issued;
           };
           int idq[S - 1];
 #pragma unroll
@@ -261,46 +302,56 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
             }
 #pragma unroll
             for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kAll, loss, m);
-            wloss += double(loss);
+            if (lane == 0) item_loss[tw + (r0 + k) * TW] = loss;
             __syncwarp();
           }
         }
         dev::cp_async_wait<0>();
-        __syncthreads();
-        combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], warp, W, lane);
-        __syncthreads();
-        update_rows<kBF16>(a.xm, a.xb, stage, (G.voff + base) * D, rows * D, threadIdx.x, blockDim.x);  // algo.hpp:651-666
-        __syncthreads();
+        team_sync();
+        combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], tw, TW, lane);
+        // the minibatch's loss in item order (rank 0, warp 0), whatever team made it
+        if (a.compute_loss && trank == 0 && warp == 0) {
+          double l = 0.0;
+          for (int i = lane; i < n_items; i += 32) l += double(__ldcg(item_loss + i));
+#pragma unroll
+          for (int m = 16; m >= 1; m >>= 1) l += __shfl_xor_sync(kAll, l, m);
+          eloss += l;
+        }
+        team_sync();
+        update_rows<kBF16>(a.xm, a.xb, stage, (G.voff + base) * D, rows * D, trank * blockDim.x + threadIdx.x,
+                           nct * blockDim.x);  // algo.hpp:651-666
+        team_sync();
       }
-      if (lane == 0) sh_loss[warp] = wloss;
-      __syncthreads();
-      if (threadIdx.x == 0 && a.compute_loss) {
-        double t = 0.0;
-        for (int w = 0; w < W; ++w) t += sh_loss[w];
-        a.loss[size_t(g) * a.epochs + e] = t;
-      }
-      __syncthreads();
+      if (threadIdx.x == 0 && trank == 0 && a.compute_loss) a.loss[size_t(g) * a.epochs + e] = eloss;
     }
-    if (a.trace && threadIdx.x == 0) a.trace[3 * g + 1] = globaltimer();
+    if (a.trace && threadIdx.x == 0 && trank == 0) a.trace[3 * g + 1] = globaltimer();
   }
 }
 
+template <int D, bool kBF16, int CT>
+BatchedKernel pick_staged_ct(int steps, int stages) {
+  if (steps == 1 && stages == 3) return staged_kernel<D, 1, 3, kBF16, CT>;
+  if (steps == 1 && stages == 4) return staged_kernel<D, 1, 4, kBF16, CT>;
+  if (steps == 2 && stages == 3) return staged_kernel<D, 2, 3, kBF16, CT>;
+  if (steps == 2 && stages == 4) return staged_kernel<D, 2, 4, kBF16, CT>;
+  return nullptr;
+}
+
 template <int D, bool kBF16>
-BatchedKernel pick_staged_fn(int steps, int stages) {
-  if (steps == 1 && stages == 3) return staged_kernel<D, 1, 3, kBF16>;
-  if (steps == 1 && stages == 4) return staged_kernel<D, 1, 4, kBF16>;
-  if (steps == 2 && stages == 3) return staged_kernel<D, 2, 3, kBF16>;
-  if (steps == 2 && stages == 4) return staged_kernel<D, 2, 4, kBF16>;
+BatchedKernel pick_staged_fn(int steps, int stages, int ctas) {
+  if (ctas == 1) return pick_staged_ct<D, kBF16, 1>(steps, stages);
+  if (ctas == 2) return pick_staged_ct<D, kBF16, 2>(steps, stages);
   return nullptr;
 }
 
 }  // namespace
 
-BatchedKernel pick_staged(int dim, bool bf16, int steps, int stages) {
+BatchedKernel pick_staged(int dim, bool bf16, int steps, int stages, int ctas) {
   switch (dim) {
-    case 32: return bf16 ? pick_staged_fn<32, true>(steps, stages) : pick_staged_fn<32, false>(steps, stages);
-    case 64: return bf16 ? pick_staged_fn<64, true>(steps, stages) : pick_staged_fn<64, false>(steps, stages);
-    case 128: return bf16 ? pick_staged_fn<128, true>(steps, stages) : pick_staged_fn<128, false>(steps, stages);
+    case 32: return bf16 ? pick_staged_fn<32, true>(steps, stages, ctas) : pick_staged_fn<32, false>(steps, stages, ctas);
+    case 64: return bf16 ? pick_staged_fn<64, true>(steps, stages, ctas) : pick_staged_fn<64, false>(steps, stages, ctas);
+    case 128:
+      return bf16 ? pick_staged_fn<128, true>(steps, stages, ctas) : pick_staged_fn<128, false>(steps, stages, ctas);
   }
   return nullptr;
 }

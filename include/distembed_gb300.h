@@ -186,6 +186,9 @@ typedef struct de_batch_shape {
   int32_t edge_cap;          /* CSR entries per work item                    */
   int32_t pairs;             /* staged kernel: warp steps in flight          */
   int32_t stages;            /* staged kernel                                */
+  int32_t team_ctas;         /* staged kernel: 2 = the largest graphs are     */
+                             /* trained by the two CTAs of a cluster together */
+                             /* (the rest one per CTA); 0 or 1 = one CTA each */
 } de_batch_shape;
 int de_batch_set_shape(de_batch *b, const de_batch_shape *shape);
 int de_batch_get_shape(const de_batch *b, de_batch_shape *shape);

@@ -61,6 +61,7 @@ def x_init(i, n, dim):
 REG = dict(kernel="register", vertices_per_warp=4, team_warps=8, edge_cap=32)
 STAGED = dict(kernel="staged", team_warps=8, edge_cap=32, pairs=2, stages=3)
 ROWS = dict(kernel="rows", team_warps=4, edge_cap=16, pairs=2, stages=3)
+CLUSTER = dict(kernel="staged", team_warps=8, edge_cap=16, pairs=2, stages=3, team_ctas=2)
 
 
 def run_batch(graphs, dim, epochs, batch, ns, lr, precision="fp32", shape=None, ids=None):
@@ -105,7 +106,8 @@ SHAPES = [dict(kernel="register", vertices_per_warp=1, team_warps=4, edge_cap=32
           dict(kernel="rows", team_warps=4, edge_cap=16, pairs=1, stages=3),
           dict(kernel="rows", team_warps=4, edge_cap=8, pairs=2, stages=4),
           dict(kernel="rows", team_warps=2, edge_cap=32, pairs=2, stages=3),
-          dict(kernel="rows", team_warps=3, edge_cap=1, pairs=1, stages=4)]
+          dict(kernel="rows", team_warps=3, edge_cap=1, pairs=1, stages=4),
+          CLUSTER, dict(CLUSTER, team_warps=4, edge_cap=8, pairs=1, stages=4)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "-".join(str(v) for v in s.values()))
@@ -118,7 +120,7 @@ def test_every_team_shape_matches_oracle(shape):
         assert np.all(np.abs(loss[i] - lo) <= LOSS_RTOL * lo), (shape, i)
 
 
-@pytest.mark.parametrize("shape", [REG, STAGED, ROWS], ids=["register", "staged", "rows"])
+@pytest.mark.parametrize("shape", [REG, STAGED, ROWS, CLUSTER], ids=["register", "staged", "rows", "cluster"])
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
 def test_alone_equals_mix_bitwise(precision, shape):
     dim, E, B, ns = 64, 3, 256, 5
@@ -157,6 +159,7 @@ def test_autotune_keeps_embeddings_and_picks_a_valid_shape():
             b.set_embeddings(i, x_init(i, n, dim))
         best, tried = b.autotune(1, B, ns, 0.02)
         assert len(tried) >= 36 and all(ms > 0 for _, ms in tried)
+        assert any(sh["team_ctas"] == 2 for sh, _ in tried)
         assert {sh["kernel"] for sh, _ in tried} == {0, 1, 2}
         assert best == min(tried, key=lambda t: t[1])[0] == b.shape()
         for i, (_, n, _, _) in enumerate(graphs):
@@ -226,7 +229,7 @@ def test_staged_rejects_more_than_32_negatives():
         assert ei.value.code == de.DE_ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("shape", [REG, STAGED, ROWS], ids=["register", "staged", "rows"])
+@pytest.mark.parametrize("shape", [REG, STAGED, ROWS, CLUSTER], ids=["register", "staged", "rows", "cluster"])
 def test_hub_rows_and_many_chunks_per_warp(shape):
     # one graph whose minibatches hold far more than 32 chunks per warp (hub rows
     # split into cap-sized pieces), so the staged pipeline restarts within a minibatch
@@ -237,3 +240,14 @@ def test_hub_rows_and_many_chunks_per_warp(shape):
     xo, lo = oracle.run(rp, c, x_init(50, n, 32), 2, 512, 6, 0.02, quirks=True)
     assert rel_l2(xs[0], xo) <= RUN_REL_L2
     assert np.all(np.abs(loss[0] - lo) <= LOSS_RTOL * lo)
+
+
+def test_cluster_teams_match_single_cta_teams_bitwise():
+    # the largest graphs of a mix go to two-CTA teams; every graph's result is the
+    # same as with one CTA per graph (same items, same order of every sum)
+    dim, E, B, ns = 64, 3, 256, 5
+    one = dict(CLUSTER, team_ctas=1)
+    xs1, l1 = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=one)
+    xs2, l2 = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=CLUSTER)
+    for i in range(len(GRAPHS)):
+        assert np.array_equal(xs1[i], xs2[i]) and np.array_equal(l1[i], l2[i]), i
