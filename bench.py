@@ -380,7 +380,7 @@ def run_bf16_form(args):
         h.set_embeddings(x0)
         loss = h.run(E, B, ns, lr, want_loss=True)   # the same job, for its losses
         pms, kind = h.profile_epoch(B, ns, lr)      # one more epoch, an event around every launch
-        names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "exact_rows", 3: "flush"}
+        names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "update_exact_rows", 3: "flush", 4: "negative_gather"}
         out[form] = {"edge_updates_per_s": sum(upd) / (sum(ms) / 1e3), "ms_per_epoch": statistics.mean(ms),
                      "loss_per_epoch": [float(v) for v in loss],
                      "profiled_epoch_ms": {names[k]: round(float(pms[kind == k].sum()), 3) for k in sorted(set(kind.tolist()))}}

@@ -282,7 +282,8 @@ class Handle:
 
     def profile_epoch(self, batch_size: int, ns: int, lr: float, first_epoch: int = 0):
         """One epoch with a CUDA event around every launch; returns (ms[], kind[])
-        (kinds: 0 minibatch/attractive kernel, 1 repulsion GEMM, 2 exact rows, 3 flush)."""
+        (kinds: 0 minibatch/attractive kernel, 1 repulsion GEMM, 2 update with exact
+        pairs, 3 flush, 4 negative gather)."""
         count = ctypes.c_int32(0)
         cap = 4 * (self.n // max(batch_size, 1) + 2) + 8
         ms = np.zeros(cap, dtype=np.float32)

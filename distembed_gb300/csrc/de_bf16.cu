@@ -103,45 +103,46 @@ __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D>
   if (mask) pair_forces<D, U, true>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
 }
 
+// The minibatch's negatives gathered once: N (k x dim), N^T (dim x k), |n|^2, ids.
+template <int D>
+__global__ void __launch_bounds__(kPlainWarps * 32) bf16_gather_kernel(const BF16BatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int epoch = a.epoch[0];
+  const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
+  const int gw = blockIdx.x * kPlainWarps + (threadIdx.x >> 5);
+  const int gws = gridDim.x * kPlainWarps;
+  if (gw == 0 && lane == 0) *a.flag_count = 0;
+  constexpr int N = D / 32;
+  for (int k = gw; k < a.kpad; k += gws) {
+    int n = k < a.ns ? __ldg(negs + k) : -1;
+    if (n >= a.n) n = -1;  // a draw equal to n contributes nothing
+    Frag<D> v;
+    if (n >= 0) load_bf16_row(v, a.xb + size_t(n) * D, lane);
+    else v.zero();
+    float sq = 0.f;
+#pragma unroll
+    for (int t = 0; t < N; ++t) {
+      const __nv_bfloat16 h = __float2bfloat16(v.v[t]);  // exact: v came from bf16
+      a.nb[size_t(k) * D + lane * N + t] = h;
+      a.nbt[size_t(lane * N + t) * a.kpad + k] = h;
+      sq = fmaf(v.v[t], v.v[t], sq);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
+    if (lane == 0) {
+      a.nn[k] = sq;
+      a.nid[k] = n;
+    }
+  }
+}
+
 template <int D, int U>
 __global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF16BatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const bool want_loss = a.compute_loss != 0;
-  const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
   const int epoch = a.epoch[0];
   const float lr = a.lr[epoch];
-
-  if (int(blockIdx.x) >= item_ctas) {
-    // ---- gather the minibatch's negatives: N (k x dim), N^T (dim x k), |n|^2, ids
-    const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
-    const int gw = (blockIdx.x - item_ctas) * kPlainWarps + wib;
-    const int gws = (gridDim.x - item_ctas) * kPlainWarps;
-    if (gw == 0 && lane == 0) *a.flag_count = 0;
-    constexpr int N = D / 32;
-    for (int k = gw; k < a.kpad; k += gws) {
-      int n = k < a.ns ? __ldg(negs + k) : -1;
-      if (n >= a.n) n = -1;  // a draw equal to n contributes nothing
-      Frag<D> v;
-      if (n >= 0) load_bf16_row(v, a.xb + size_t(n) * D, lane);
-      else v.zero();
-      float sq = 0.f;
-#pragma unroll
-      for (int t = 0; t < N; ++t) {
-        const __nv_bfloat16 h = __float2bfloat16(v.v[t]);  // exact: v came from bf16
-        a.nb[size_t(k) * D + lane * N + t] = h;
-        a.nbt[size_t(lane * N + t) * a.kpad + k] = h;
-        sq = fmaf(v.v[t], v.v[t], sq);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
-      if (lane == 0) {
-        a.nn[k] = sq;
-        a.nid[k] = n;
-      }
-    }
-    return;
-  }
 
   const int gw = blockIdx.x * kPlainWarps + wib;
   if (gw >= a.n_items) return;
@@ -546,42 +547,23 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         *reinterpret_cast<float4 *>(dst + 4) = make_float4(g[4], g[5], g[6], g[7]);
       }
     }
-    int *row_flags = reinterpret_cast<int *>(sC_ptr[1]);  // 1: update x, 2: defer to abuf
+    int *row_flags = reinterpret_cast<int *>(sC_ptr[1]);  // nonzero: the row's force is final
     if (hf == 0) row_flags[t] = (row_valid && done) ? (near ? 2 : 1) : 0;
     epi_sync();
 
-    // Coalesced update, one warp per row, each lane 8 consecutive dims:
-    // x += abuf + lr * force, or abuf += lr * force for rows finished by
-    // bf16_fixup_kernel.
+    // Coalesced store of lr * force, one warp per row, each lane D/32 consecutive
+    // dims, into rbuf; bf16_apply_kernel adds it to the row together with the
+    // attractive update (which runs concurrently into abuf).
     constexpr int kPer = D / 32;
     for (int rr = warp; rr < kTileRows; rr += kEpiThreads / 32) {
-      const int flag = row_flags[rr];
-      if (flag == 0) continue;
+      if (row_flags[rr] == 0) continue;
       const int rl = tile_base + rr;
-      const size_t rg = size_t(a.base + rl);
       const float *src = stage + rr * kPitch + lane * kPer;
-      float *abp = a.abuf + size_t(rl) * D + lane * kPer;
-      float *xmp = a.xm + rg * D + lane * kPer;
-      __nv_bfloat16 *xbp = a.xb + rg * D + lane * kPer;
-      float pv[kPer];
+      float *rbp = a.rbuf + size_t(rl) * D + lane * kPer;
 #pragma unroll
       for (int q = 0; q < kPer; q += 2) {
-        const float2 ab2 = *reinterpret_cast<const float2 *>(abp + q);
         const float2 f2 = *reinterpret_cast<const float2 *>(src + q);
-        pv[q] = ab2.x + lr * f2.x;
-        pv[q + 1] = ab2.y + lr * f2.y;
-      }
-      if (flag == 2) {
-#pragma unroll
-        for (int q = 0; q < kPer; q += 2) *reinterpret_cast<float2 *>(abp + q) = make_float2(pv[q], pv[q + 1]);
-      } else {
-#pragma unroll
-        for (int q = 0; q < kPer; q += 2) {
-          const float2 m2 = *reinterpret_cast<const float2 *>(xmp + q);
-          const float m0 = m2.x + pv[q], m1 = m2.y + pv[q + 1];
-          *reinterpret_cast<float2 *>(xmp + q) = make_float2(m0, m1);
-          *reinterpret_cast<__nv_bfloat162 *>(xbp + q) = __floats2bfloat162_rn(m0, m1);
-        }
+        *reinterpret_cast<float2 *>(rbp + q) = make_float2(lr * f2.x, lr * f2.y);
       }
     }
   }
@@ -595,63 +577,80 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   }
 }
 
-// ------------------------------------------------------------ exact rows
+// ------------------------------------------------------------ update
 
-// Rows with exact-path pairs: one warp per row adds those pairs in FP32 on the
-// BF16 values with the per-component clip (algo.hpp:633-645), in negative
-// order, to the GEMM part of the update left in abuf, then updates the row and
-// clears its bitmask.
+// One warp per row of the minibatch: x += abuf + rbuf (attractive and GEMM
+// repulsive updates, algo.hpp:651-666), plus, for a row with exact-path pairs
+// (bitmask bits), those pairs added in FP32 on the BF16 values with the
+// per-component clip (algo.hpp:633-645), in negative order; the bits are cleared.
 template <int D>
-__global__ void __launch_bounds__(256) bf16_fixup_kernel(const BF16BatchArgs a) {
+__global__ void __launch_bounds__(256) bf16_apply_kernel(const BF16BatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int count = *a.flag_count;
   const int epoch = a.epoch[0];
   const float lr = a.lr[epoch];
   constexpr int N = D / 32;
-  for (int s = gw; s < count; s += gridDim.x * 8) {
-    const int row_local = a.flag_rows[s];
+  for (int row_local = gw; row_local < a.rows; row_local += gridDim.x * 8) {
     const int row = a.base + row_local;
     uint32_t *bits_row = a.near_bits + size_t(row_local) * kNearWords;
     const uint32_t my_word = lane < kNearWords ? bits_row[lane] : 0u;
-    Frag<D> xi, acc;
-    load_bf16_row(xi, a.xb + size_t(row) * D, lane);
+    Frag<D> acc;
     acc.zero();
-    float loss = 0.f;
-    for (int w = 0; w < kNearWords; ++w) {
-      uint32_t bits = __shfl_sync(kFull, my_word, w);
-      while (bits) {
-        const int i = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const int k = (w >> 1) * kChunk + (w & 1) * 32 + i;  // word w = 2 * chunk + half
-        Frag<D> xn;
-        load_bf16_row(xn, a.nb + size_t(k) * D, lane);
-        float diff[N];
-        float p = 0.f;
+    const bool exact = __any_sync(kFull, my_word != 0u);
+    if (exact) {
+      Frag<D> xi;
+      load_bf16_row(xi, a.xb + size_t(row) * D, lane);
+      float loss = 0.f;
+      for (int w = 0; w < kNearWords; ++w) {
+        uint32_t bits = __shfl_sync(kFull, my_word, w);
+        while (bits) {
+          const int i = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const int k = (w >> 1) * kChunk + (w & 1) * 32 + i;  // word w = 2 * chunk + half
+          Frag<D> xn;
+          load_bf16_row(xn, a.nb + size_t(k) * D, lane);
+          float diff[N];
+          float p = 0.f;
 #pragma unroll
-        for (int t = 0; t < N; ++t) {
-          diff[t] = xi.v[t] - xn.v[t];
-          p = fmaf(diff[t], diff[t], p);
+          for (int t = 0; t < N; ++t) {
+            diff[t] = xi.v[t] - xn.v[t];
+            p = fmaf(diff[t], diff[t], p);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
+          const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
+#pragma unroll
+          for (int t = 0; t < N; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
+          loss += logf((1.0f + p) / (p + 1e-6f));
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
-        const float c = 2.0f / ((p + 1e-6f) * (1.0f + p));
-#pragma unroll
-        for (int t = 0; t < N; ++t) acc.v[t] = fmaf(lr, clip(diff[t] * c, a.bound), acc.v[t]);
-        loss += logf((1.0f + p) / (p + 1e-6f));
       }
+      if (lane < kNearWords) bits_row[lane] = 0u;
+      if (lane == 0) a.loss_row[row] += double(loss);
     }
-    if (lane < kNearWords) bits_row[lane] = 0u;
+    // lane: N consecutive components, moved as float2 / bf16x2 pairs
     float *xm = a.xm + size_t(row) * D + lane * N;
     __nv_bfloat16 *xb = a.xb + size_t(row) * D + lane * N;
     const float *ab = a.abuf + size_t(row_local) * D + lane * N;
+    const float *rb = a.rbuf + size_t(row_local) * D + lane * N;
+    float mv[N];
 #pragma unroll
-    for (int t = 0; t < N; ++t) {
-      const float m = xm[t] + ab[t] + acc.v[t];
-      xm[t] = m;
-      xb[t] = __float2bfloat16(m);
+    for (int t = 0; t < N; t += 2) {
+      const float2 x2 = __ldcg(reinterpret_cast<const float2 *>(xm + t));
+      const float2 a2 = __ldcg(reinterpret_cast<const float2 *>(ab + t));
+      const float2 r2 = __ldcg(reinterpret_cast<const float2 *>(rb + t));
+      mv[t] = x2.x + (a2.x + r2.x);
+      mv[t + 1] = x2.y + (a2.y + r2.y);
     }
-    if (lane == 0) a.loss_row[row] += double(loss);
+#pragma unroll
+    for (int t = 0; t < N; t += 2) {
+      float m0 = mv[t], m1 = mv[t + 1];
+      if (exact) {
+        m0 = m0 + acc.v[t];
+        m1 = m1 + acc.v[t + 1];
+      }
+      *reinterpret_cast<float2 *>(xm + t) = make_float2(m0, m1);
+      *reinterpret_cast<__nv_bfloat162 *>(xb + t) = __floats2bfloat162_rn(m0, m1);
+    }
   }
 }
 
@@ -722,35 +721,50 @@ cudaError_t bf16_prepare(int dim) {
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev) {
+namespace {
+
+template <int D, int U>
+cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
+                                const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                                cudaEvent_t fork, cudaEvent_t join) {
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
-  const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps < 64 ? (a.kpad + kPlainWarps - 1) / kPlainWarps : 64;
+  const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps;  // one warp per negative
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
-  const int fix_ctas = 128;
-  auto mark = [&](int i) {
-    if (ev) cudaEventRecord(ev[i], s);
-  };
-  switch (dim) {
-    case 64:
-      mark(0); bf16_attract_kernel<64, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      mark(1); bf16_repulse_kernel<64><<<tiles, kRepulseThreads, RepulseSmem<64>::dynamic, s>>>(mx, mn, mt, a);
-      mark(2); bf16_fixup_kernel<64><<<fix_ctas, 256, 0, s>>>(a);
-      break;
-    case 128:
-      mark(0); bf16_attract_kernel<128, 8><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      mark(1); bf16_repulse_kernel<128><<<tiles, kRepulseThreads, RepulseSmem<128>::dynamic, s>>>(mx, mn, mt, a);
-      mark(2); bf16_fixup_kernel<128><<<fix_ctas, 256, 0, s>>>(a);
-      break;
-    case 256:
-      mark(0); bf16_attract_kernel<256, 4><<<item_ctas + gather_ctas, kPlainWarps * 32, 0, s>>>(a);
-      mark(1); bf16_repulse_kernel<256><<<tiles, kRepulseThreads, RepulseSmem<256>::dynamic, s>>>(mx, mn, mt, a);
-      mark(2); bf16_fixup_kernel<256><<<fix_ctas, 256, 0, s>>>(a);
-      break;
-    default:
-      return cudaErrorInvalidValue;
+  const int apply_ctas = (a.rows + 7) / 8;
+  cudaError_t e = cudaSuccess;
+  if (ev || !s2) {  // one after another (per-kernel timing)
+    if (ev) cudaEventRecord(ev[0], s);
+    bf16_gather_kernel<D><<<gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[1], s);
+    bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[2], s);
+    bf16_repulse_kernel<D><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s>>>(mx, mn, mt, a);
+    if (ev) cudaEventRecord(ev[3], s);
+    bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
+    return cudaGetLastError();
   }
+  // the attractive pass and the repulsion GEMMs are independent within a
+  // minibatch: they run on two streams, joined before the update
+  bf16_gather_kernel<D><<<gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+  if ((e = cudaEventRecord(fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(s2, fork, 0)) != cudaSuccess) return e;
+  bf16_repulse_kernel<D><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s2>>>(mx, mn, mt, a);
+  bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
+  if ((e = cudaEventRecord(join, s2)) != cudaSuccess || (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
+  bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
+                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                              cudaEvent_t fork, cudaEvent_t join) {
+  switch (dim) {
+    case 64: return launch_bf16_batch_d<64, 8>(a, mx, mn, mt, s, ev, s2, fork, join);
+    case 128: return launch_bf16_batch_d<128, 8>(a, mx, mn, mt, s, ev, s2, fork, join);
+    case 256: return launch_bf16_batch_d<256, 4>(a, mx, mn, mt, s, ev, s2, fork, join);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s) {

@@ -110,6 +110,7 @@ struct BF16BatchArgs {
   float *P;                 // partial slots of split rows
   int32_t *counters;
   float *abuf;              // [B, dim] attractive update of the minibatch (lr applied)
+  float *rbuf;              // [B, dim] repulsive (GEMM) update of the minibatch (lr applied)
   __nv_bfloat16 *nb;        // [kpad, dim] gathered negatives
   __nv_bfloat16 *nbt;       // [dim, kpad] the same, transposed
   float *nn;                // [kpad] squared norms of the gathered negatives
@@ -138,10 +139,14 @@ struct BF16FlushArgs {
 // BF16 launchers (de_bf16.cu).
 int bf16_repulse_smem_bytes(int dim);
 cudaError_t bf16_prepare(int dim);
-// ev (nullable): three events recorded before the attractive, repulsive and
-// exact-row launches of the minibatch.
+// One minibatch: gather of the negatives, then the attractive pass (on s) and the
+// repulsion GEMMs (on s2, forked and joined with the two events), then the
+// update with the exact close pairs.  ev (nullable): four events recorded before
+// the gather, attractive, GEMM and update launches, all on s one after another
+// (so is everything when s2 is null).
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev);
+                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                              cudaEvent_t fork, cudaEvent_t join);
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
 cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
 

@@ -91,6 +91,10 @@ struct de_handle {
   __nv_bfloat16 *d_xb = nullptr;
   float *d_abuf = nullptr;
   size_t abuf_cap = 0;
+  float *d_rbuf = nullptr;
+  size_t rbuf_cap = 0;
+  cudaStream_t stream2 = nullptr;  // the repulsion GEMMs, forked from and joined to `stream`
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   __nv_bfloat16 *d_nb = nullptr, *d_nbt = nullptr;
   size_t nb_cap = 0;
   float *d_nn = nullptr;
@@ -328,6 +332,7 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.P = h->d_parts;
     a.counters = h->d_counters;
     a.abuf = h->d_abuf;
+    a.rbuf = h->d_rbuf;
     a.nb = h->d_nb;
     a.nbt = h->d_nbt;
     a.nn = h->d_nn;
@@ -339,7 +344,8 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.loss_off = s.item_off[j];
     a.loss_row = h->d_loss_row;
     a.err = h->d_err;
-    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st, ev ? ev + 3 * j : nullptr);
+    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st, ev ? ev + 4 * j : nullptr, h->stream2,
+                            h->ev_fork, h->ev_join);
   }
   if (err == cudaSuccess) {
     BF16FlushArgs f{};
@@ -352,7 +358,7 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     f.loss = h->d_loss;
     f.epoch = h->d_epoch;
     f.compute_loss = h->opt.compute_loss;
-    if (ev) cudaEventRecord(ev[3 * s.batches], st);
+    if (ev) cudaEventRecord(ev[4 * s.batches], st);
     err = launch_bf16_flush(f, st);
   }
   return err;
@@ -366,6 +372,7 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
   bool m = false, near_moved = false;
   int rc = DE_OK;
   if ((rc = grow(h, &h->d_abuf, &h->abuf_cap, size_t(s.batch) * h->dim, &m)) ||
+      (rc = grow(h, &h->d_rbuf, &h->rbuf_cap, size_t(s.batch) * h->dim, &m)) ||
       (rc = grow(h, &h->d_flag_rows, &h->flag_cap, size_t(s.batch), &m)) ||
       (rc = grow(h, &h->d_near_bits, &h->near_cap, size_t(s.batch) * 32, &near_moved)))
     return rc;
@@ -463,7 +470,7 @@ cudaError_t enqueue_epoch_plain(de_handle *h, int ns, cudaStream_t st, cudaEvent
 std::vector<int> epoch_launch_kinds(const de_handle *h) {
   std::vector<int> k;
   if (h->opt.precision == DE_PRECISION_BF16)
-    for (int j = 0; j < h->sched.batches; ++j) k.insert(k.end(), {0, 1, 2});
+    for (int j = 0; j < h->sched.batches; ++j) k.insert(k.end(), {4, 0, 1, 2});
   else
     k.assign(h->sched.batches, 0);
   k.push_back(3);
@@ -615,7 +622,10 @@ int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t 
         (e = cudaMemsetAsync(h->d_xb, 0, size_t(n) * dim * sizeof(__nv_bfloat16), h->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(h->d_loss_row, 0, size_t(n) * sizeof(double), h->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(h->stream)) != cudaSuccess ||
-        (e = bf16_prepare(dim)) != cudaSuccess)
+        (e = bf16_prepare(dim)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming)) != cudaSuccess)
       return bail(cuda_fail(h.get(), e, "BF16 form set-up"));
   }
   *out = h.release();
@@ -653,6 +663,7 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->d_flag_count);
   dev_free(h, h->d_xb);
   dev_free(h, h->d_abuf);
+  dev_free(h, h->d_rbuf);
   dev_free(h, h->d_nb);
   dev_free(h, h->d_nbt);
   dev_free(h, h->d_nn);
@@ -670,6 +681,12 @@ int de_destroy(de_handle *h) {
   if (h->h_loss) host_free(h, h->h_loss);
   if (h->h_epoch) host_free(h, h->h_epoch);
   if (h->upload_done) cudaEventDestroy(h->upload_done);
+  if (h->stream2) {
+    cudaStreamSynchronize(h->stream2);
+    cudaStreamDestroy(h->stream2);
+  }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return DE_OK;

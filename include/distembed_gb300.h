@@ -102,7 +102,9 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
  * but launches its kernels one by one with CUDA events between them and waits:
  * launch_ms[i] is the device time of launch i and launch_kind[i] its kind (0: the
  * minibatch kernel of the FP32 form / the attractive kernel of the BF16 form,
- * 1: BF16 repulsion GEMM kernel, 2: BF16 exact-row kernel, 3: epoch flush).
+ * 1: BF16 repulsion GEMM kernel, 2: BF16 update with the exact close pairs,
+ * 3: epoch flush, 4: BF16 negative gather); the launches of the profiled epoch
+ * run one after another (the BF16 attractive pass and GEMMs are not overlapped).
  * *count receives the number of launches; capacity must be at least that.  The
  * epoch is a real step: the embedding is updated.  No reference counterpart:
  * this is the per-kernel timing used by the benchmark. */
