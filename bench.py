@@ -513,6 +513,7 @@ def run_batched_form(args):
     bf = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="fp32")
     try:
         bf.set_shape(**shape)
+        bf.prepare(E, B, ns, lr)
     except de.DEError:  # the shape's FP32 rows do not fit in shared memory: the autotuner picks one
         bf.autotune(1, B, ns, lr)
     bf.set_embeddings(-1, x0_all)
