@@ -370,29 +370,80 @@ def run_bf16_form(args):
     x0 = gg.init_embedding(n, W3["dim"], seed=W3["init_seed"]).astype(np.float32)
     gen_s = time.perf_counter() - t0
     dim, B, ns, lr, E = W3["dim"], W3["batch"], W3["ns"], W3["lr"], W3["epochs"]
-    out = {}
+    batches = -(-n // B)
+    out, clk, e2e = {}, None, None
+    names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "update_exact_rows", 3: "flush", 4: "negative_gather"}
     for form in ("fp32", "bf16"):
         h = de.Handle(rowptr, col, dim, precision=form, quirks=True, compute_loss=True, pdl=bool(args.pdl))
         stream = torch.cuda.ExternalStream(h.stream, device=0)
         h.set_embeddings(x0)
         upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
+        clocks = Clocks(0)
+        if form == "bf16":
+            clocks.start()
         ms = timed_job(h, E, B, ns, lr, stream, warmup=1)
+        if form == "bf16":
+            clk = clocks.stop()
         h.set_embeddings(x0)
         loss = h.run(E, B, ns, lr, want_loss=True)   # the same job, for its losses
         pms, kind = h.profile_epoch(B, ns, lr)      # one more epoch, an event around every launch
-        names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "update_exact_rows", 3: "flush", 4: "negative_gather"}
         out[form] = {"edge_updates_per_s": sum(upd) / (sum(ms) / 1e3), "ms_per_epoch": statistics.mean(ms),
                      "loss_per_epoch": [float(v) for v in loss],
                      "profiled_epoch_ms": {names[k]: round(float(pms[kind == k].sum()), 3) for k in sorted(set(kind.tolist()))}}
+        if form == "bf16" and args.e2e_steps > 0:
+            # end to end through the public API: pinned host FP32 in, the 10-epoch job, host FP32 out
+            x_host = torch.empty((n, dim), dtype=torch.float32, pin_memory=True).numpy()
+            x_host[:] = x0
+            o_host = torch.empty((n, dim), dtype=torch.float32, pin_memory=True).numpy()
+            ts = []
+            for k in range(args.e2e_steps + 1):
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                h.set_embeddings(x_host)
+                h.run(E, B, ns, lr, want_loss=False)
+                h.get_embeddings(out=o_host)
+                if k > 0:
+                    ts.append(time.perf_counter() - t1)
+            e2e = {"value": sum(upd) / statistics.mean(ts), "unit": UNIT, "h2d_bytes_per_step": n * dim * 4,
+                   "d2h_bytes_per_step": n * dim * 4, "ms_per_step": 1e3 * statistics.mean(ts),
+                   "step": "host FP32 embedding in (pinned), the 10-epoch job, host FP32 embedding out"}
         h.close()
+    # rooflines from the per-launch event times of the profiled BF16 epoch
+    prof = out["bf16"]["profiled_epoch_ms"]
+    rows_total = n  # every vertex is a GEMM row once per epoch (quirks: the repulsive rows of
+    #                 the last minibatch are last_batch_size, the same count)
+    kpad = max(64, -(-ns // 64) * 64)
+    gemm_flops = 4.0 * rows_total * kpad * dim
+    tflops = gemm_flops / (prof["repulsion_gemm"] / 1e3) / 1e12
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        tpeak, tsrc = float(peaks["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        tpeak, tsrc = 1900.0, "fallback"
+    nnz_eff = int(len(col))
+    attr_bytes = nnz_eff * (4 + 2 * dim) + n * (8 + 2 * dim + 4 * dim)
+    hpeak, hsrc = measured_peak()
+    attr_gbs = attr_bytes / (prof["minibatch/attractive"] / 1e3) / 1e9
+    roof_gemm = {"bound": "tensor", "kernel": "bf16_repulse_kernel<256>", "achieved": tflops, "peak": tpeak,
+                 "unit": "TFLOP/s", "frac": tflops / tpeak, "peak_source": tsrc, "traffic": None,
+                 "algorithmic_flops_per_epoch": gemm_flops,
+                 "note": "4 x rows x kpad x dim per epoch (two GEMMs) / summed event time of the GEMM launches"}
+    roof_attr = {"bound": "hbm", "kernel": "bf16_attract_kernel<256>", "achieved": attr_gbs, "peak": hpeak,
+                 "unit": "GB/s", "frac": attr_gbs / hpeak, "peak_source": hsrc,
+                 "algorithmic_bytes_per_epoch": attr_bytes,
+                 "note": "per CSR entry: column id + BF16 neighbour row; per vertex: rowptr, own BF16 row, FP32 update row"}
+    dominant_gemm = prof["repulsion_gemm"] >= prof["minibatch/attractive"]
     gap = abs(out["bf16"]["loss_per_epoch"][-1] - out["fp32"]["loss_per_epoch"][-1]) / out["fp32"]["loss_per_epoch"][-1]
     line = {"metric": METRIC, "value": out["bf16"]["edge_updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": E,
             "warmup": 1, "ms_per_step": out["bf16"]["ms_per_epoch"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16",
-            "data": "synthetic: R-MAT scale 22 (ef 16, a.57 b.19 c.19, seed 2), U[-0.5,0.5] init (seed 0)",
+            "data": f"synthetic: R-MAT scale {scale} (ef 16, a.57 b.19 c.19, seed 2), U[-0.5,0.5] init (seed 0)",
             "config": {"workload": (WORKLOAD3 if scale == W3["scale"] else f"rmat{scale}_ef16_d256_b8192_ns1024") + "_bf16", "n": n, "nnz": int(len(col)), "dim": dim, "batch": B,
-                       "ns": ns, "lr": lr, "epochs_per_job": E, "step": "one epoch (512 minibatches)",
+                       "ns": ns, "lr": lr, "epochs_per_job": E, "step": f"one epoch ({-(-n // B)} minibatches)",
                        "generate_s": round(gen_s, 1)},
+            "roofline": roof_gemm if dominant_gemm else roof_attr,
+            "roofline_other": roof_attr if dominant_gemm else roof_gemm,
+            "e2e": e2e, "clocks": clk, "gpu_launches": E * (4 * batches + 1),
             "compare": {"fp32_plain": {k: v for k, v in out["fp32"].items()}, "bf16": out["bf16"],
                         "bf16_over_fp32": out["bf16"]["edge_updates_per_s"] / out["fp32"]["edge_updates_per_s"],
                         "final_loss_gap_vs_fp32": gap}}

@@ -73,6 +73,30 @@ static __device__ __forceinline__ long long globaltimer() {
 
 static __device__ __forceinline__ float bclip(float v, float b) { return v > b ? b : (v < -b ? -b : v); }
 
+// d = x - y over 8 components with packed f32x2 arithmetic; returns |d|^2 (two
+// interleaved partial sums, then their sum).
+static __device__ __forceinline__ float diff8(float (&d)[8], const float (&x)[8], const float (&y)[8]) {
+  float2 q = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int t = 0; t < 8; t += 2) {
+    const float2 v = dev::sub2(make_float2(x[t], x[t + 1]), make_float2(y[t], y[t + 1]));
+    d[t] = v.x;
+    d[t + 1] = v.y;
+    q = __ffma2_rn(v, v, q);
+  }
+  return q.x + q.y;
+}
+
+// acc += s * d over 8 components (packed f32x2 FMA).
+static __device__ __forceinline__ void axpy8(float (&acc)[8], float s, const float (&d)[8]) {
+#pragma unroll
+  for (int t = 0; t < 8; t += 2) {
+    const float2 o = __ffma2_rn(make_float2(s, s), make_float2(d[t], d[t + 1]), make_float2(acc[t], acc[t + 1]));
+    acc[t] = o.x;
+    acc[t + 1] = o.y;
+  }
+}
+
 // x[row0 + i] += stage[i] for i < count (and the BF16 copy), every thread's
 // loads issued before its stores.
 template <bool kBF16>

@@ -36,13 +36,7 @@ __device__ __forceinline__ void rows_steps(const BatchedArgs &a, float (&acc)[8]
 #pragma unroll
       for (int t = 0; t < 8; ++t) xn[t] = xi[t];
     }
-    float p = 0.f;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      d[st][t] = xi[t] - xn[t];
-      p = fmaf(d[st][t], d[st][t], p);
-    }
-    r[st] = p;
+    r[st] = diff8(d[st], xi, xn);
     ok[st] = in && valid(sidx);
   }
 #pragma unroll
@@ -65,11 +59,7 @@ __device__ __forceinline__ void rows_steps(const BatchedArgs &a, float (&acc)[8]
           const float4 *srcp = reinterpret_cast<const float4 *>(a.xm + (voff + gv) * D + gl * 8);
           const float4 x = __ldcg(srcp), y = __ldcg(srcp + 1);
           const float f[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            d[st][t] = xi[t] - f[t];
-            p = fmaf(d[st][t], d[st][t], p);
-          }
+          p = diff8(d[st], xi, f);
         }
 #pragma unroll
         for (int m = LP / 2; m >= 1; m >>= 1) p += __shfl_xor_sync(kAll, p, m);
@@ -89,9 +79,7 @@ __device__ __forceinline__ void rows_steps(const BatchedArgs &a, float (&acc)[8]
   if (!__any_sync(kAll, may_clip)) {
 #pragma unroll
     for (int st = 0; st < NS; ++st) {
-      const float lc = lr * c[st];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc[t] = fmaf(lc, d[st][t], acc[t]);
+      axpy8(acc, lr * c[st], d[st]);
     }
   } else {
 #pragma unroll

@@ -54,13 +54,7 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
 #pragma unroll
       for (int t = 0; t < 8; ++t) xn[t] = xi[t];
     }
-    float p = 0.f;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      d[st][t] = xi[t] - xn[t];
-      p = fmaf(d[st][t], d[st][t], p);
-    }
-    r[st] = p;
+    r[st] = diff8(d[st], xi, xn);
     ok[st] = k[st] < count && ((vmask >> k[st]) & 1u);
   }
 #pragma unroll
@@ -83,11 +77,7 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
           const float4 *src = reinterpret_cast<const float4 *>(a.xm + (voff + gid) * D + gl * 8);
           const float4 x = __ldcg(src), y = __ldcg(src + 1);
           const float f[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            d[st][t] = xi[t] - f[t];
-            p = fmaf(d[st][t], d[st][t], p);
-          }
+          p = diff8(d[st], xi, f);
         }
 #pragma unroll
         for (int m = LP / 2; m >= 1; m >>= 1) p += __shfl_xor_sync(kAll, p, m);
@@ -107,9 +97,7 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
   if (!__any_sync(kAll, may_clip)) {
 #pragma unroll
     for (int st = 0; st < NS; ++st) {
-      const float lc = lr * c[st];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc[t] = fmaf(lc, d[st][t], acc[t]);
+      axpy8(acc, lr * c[st], d[st]);
     }
   } else {
 #pragma unroll

@@ -126,26 +126,44 @@ __device__ __forceinline__ float multi_warp_sum(float (&p)[U], int lane) {
   return r;
 }
 
+// Packed FP32 pair arithmetic (Blackwell f32x2 FMA: two lanes of work per
+// instruction).  sub2(a, b) = a - b exactly as a scalar subtraction rounds it.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
 // U pair forces between x_i and rows xn[0..U): valid_mask bit u says whether
 // pair u counts (invalid pairs must carry xn[u] == xi).  Attractive:
 // c = -2/(1+r); repulsive: c = 2/((r+1e-6)(1+r)) (algo.hpp:573, 626/641).
-// Each component is clipped and accumulated in pair order.  The loss term of a
-// pair is added on the lane that holds its full sum (FP32 within one work
-// item; the caller folds it into the FP64 epoch sum).
+// Each component is clipped (algo.hpp:65-72) and accumulated in pair order.
+// Clip-free fast path: |c (x_d - n_d)| <= |c| sqrt(r), so no component can reach
+// the bound when c^2 r <= bound^2 and the clip is the identity.  For the
+// attractive force |c| sqrt(r) = 2 sqrt(r) / (1 + r) <= 1, so any bound >= 1
+// never clips; for repulsion the warp takes the clipped path when any of its
+// pairs has c^2 r above 0.98 bound^2.  The loss term of a pair is added on the
+// lane that holds its full sum (FP32 within one work item; the caller folds it
+// into the FP64 epoch sum).
 template <int D, int U, bool kAttract>
 __device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, const Frag<D> (&xn)[U],
                                             unsigned valid_mask, float lr, float bound, bool want_loss,
                                             float &loss, int lane) {
   constexpr int L = Log2<U>::value;
-  float diff[U][Frag<D>::N];
+  constexpr int N = Frag<D>::N;
+  float diff[U][N];
   float p[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    p[u] = 0.f;
+    if constexpr (N >= 2) {
+      float2 q = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int t = 0; t < Frag<D>::N; ++t) {
-      diff[u][t] = xi.v[t] - xn[u].v[t];
-      p[u] = fmaf(diff[u][t], diff[u][t], p[u]);
+      for (int t = 0; t < N; t += 2) {
+        const float2 d = sub2(make_float2(xi.v[t], xi.v[t + 1]), make_float2(xn[u].v[t], xn[u].v[t + 1]));
+        diff[u][t] = d.x;
+        diff[u][t + 1] = d.y;
+        q = __ffma2_rn(d, d, q);
+      }
+      p[u] = q.x + q.y;
+    } else {
+      diff[u][0] = xi.v[0] - xn[u].v[0];
+      p[u] = diff[u][0] * diff[u][0];
     }
   }
   const float r = multi_warp_sum<U>(p, lane);
@@ -155,11 +173,30 @@ __device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, con
   if (!valid) c = 0.f;
   if (want_loss && valid && (lane & ((32 >> L) - 1)) == 0)
     loss += kAttract ? log1pf(r) : logf((1.0f + r) / (r + 1e-6f));
+  const bool no_clip = kAttract ? bound >= 1.0f : !__any_sync(kFull, c * c * r > 0.98f * bound * bound);
+  if (no_clip) {
 #pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const float cu = __shfl_sync(kFull, c, u << (5 - L));
+    for (int u = 0; u < U; ++u) {
+      const float lc = lr * __shfl_sync(kFull, c, u << (5 - L));
+      if constexpr (N >= 2) {
 #pragma unroll
-    for (int t = 0; t < Frag<D>::N; ++t) acc.v[t] = fmaf(lr, clip(diff[u][t] * cu, bound), acc.v[t]);
+        for (int t = 0; t < N; t += 2) {
+          const float2 o = __ffma2_rn(make_float2(lc, lc), make_float2(diff[u][t], diff[u][t + 1]),
+                                      make_float2(acc.v[t], acc.v[t + 1]));
+          acc.v[t] = o.x;
+          acc.v[t + 1] = o.y;
+        }
+      } else {
+        acc.v[0] = fmaf(lc, diff[u][0], acc.v[0]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const float cu = __shfl_sync(kFull, c, u << (5 - L));
+#pragma unroll
+      for (int t = 0; t < N; ++t) acc.v[t] = fmaf(lr, clip(diff[u][t] * cu, bound), acc.v[t]);
+    }
   }
 }
 

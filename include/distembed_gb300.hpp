@@ -14,7 +14,10 @@
  * and writes the embedding back in place, as the reference does.  receiver,
  * sender, grid, alpha, beta and sync_comm steer the multi-rank exchange, which
  * one resident partition does not have: they are accepted and not used.
- * col_major (the transposed traversal, algo.hpp:450-518) is not provided.
+ * col_major is accepted and does not change the result: the reference's one-rank
+ * branch calls the attractive pass with col_major = false whatever the flag
+ * (cpp/algo/algo.hpp:184-186); the transposed traversal (algo.hpp:450-518) runs
+ * only in the multi-rank exchange.
  *
  * Errors throw distembed_gb300::Error (a std::runtime_error) with the library's
  * message, where the reference prints and exits.
@@ -101,7 +104,7 @@ class GpuEmbeddingAlgo {
  private:
   void init(int64_t n, const int64_t *rowptr, const int64_t *col, VALUE_TYPE *coordinates, VALUE_TYPE max_bound,
             VALUE_TYPE min_bound, bool col_major, int precision, int device) {
-    if (col_major) throw Error(DE_ERR_UNSUPPORTED, "col_major traversal is not provided");
+    (void)col_major;  // one rank: the row-major pass whatever the flag (algo.hpp:184-186)
     if (min_bound != -max_bound) throw Error(DE_ERR_INVALID, "the bounds must be [-MAX_BOUND, MAX_BOUND]");
     de_options o;
     de_default_options(&o);

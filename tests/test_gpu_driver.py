@@ -68,3 +68,20 @@ def test_driver_matches_api_and_oracle(tmp_path, dim):
     xo, _ = oracle.run(rp, col, x0, E, B, ns, lr, quirks=True)
     assert np.linalg.norm(xa - xo) / np.linalg.norm(xo) <= 1e-4
     assert os.path.exists(tmp_path / "perf_output")
+
+
+def test_driver_col_major_flag_is_the_one_rank_row_major_pass(tmp_path):
+    """-col_major 1 writes the same file: the reference's one-rank branch calls the
+    attractive pass with col_major = false (cpp/algo/algo.hpp:184-186)."""
+    n, rp, col = gg.knn_csr(800, 16, 8, 4, seed=7)
+    mtx = str(tmp_path / "g.mtx")
+    gg.write_mtx(mtx, n, rp, col)
+    texts = []
+    for cm in ("0", "1"):
+        out = tmp_path / f"out{cm}"
+        out.mkdir()
+        r = subprocess.run([de.DRIVER_PATH, "-input", mtx, "-output", str(out), "-iter", "3", "-batch", "128",
+                            "-dim", "64", "-col_major", cm], capture_output=True, text=True, cwd=str(tmp_path))
+        assert r.returncode == 0, r.stderr
+        texts.append((out / "embedding.txt").read_text())
+    assert texts[0] == texts[1]
