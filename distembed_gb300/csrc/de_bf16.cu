@@ -15,12 +15,14 @@
 // when no component can reach the bound: |c (x_d - n_d)| <= c sqrt(r) < 5 for
 // r >= 0.25.  A pair with r < 0.25 (other than a row drawn as its own negative,
 // whose force is exactly zero) is left out of the GEMMs and recorded in a
-// per-row bitmask; bf16_fixup_kernel adds those pairs one by one in FP32 with the
-// clip, then updates the row.
+// per-row bitmask; the update kernel adds those pairs one by one in FP32 with
+// the clip.
 //
-// Per minibatch: bf16_attract_kernel (attractive pass, warp per work item, plus
-// CTAs that gather the negatives into N / N^T), bf16_repulse_kernel (GEMMs and the
-// update of every unflagged row), bf16_fixup_kernel (flagged rows).
+// Per minibatch: bf16_gather_kernel (the negatives into N, N^T, |n|^2), then
+// bf16_attract_kernel (attractive pass, warp per work item) and
+// bf16_repulse_kernel (the GEMMs), which are independent and run on two
+// streams, then bf16_apply_kernel (exact close pairs and the update of every
+// row of the minibatch).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -78,8 +80,13 @@ template <int D>
 __device__ __forceinline__ void store_f32_contig(const Frag<D> &f, float *row, int lane) {
   constexpr int N = D / 32;
   float *p = row + lane * N;
+  if constexpr (N % 4 == 0) {
 #pragma unroll
-  for (int i = 0; i < N; i += 2) *reinterpret_cast<float2 *>(p + i) = make_float2(f.v[i], f.v[i + 1]);
+    for (int i = 0; i < N; i += 4) *reinterpret_cast<float4 *>(p + i) = make_float4(f.v[i], f.v[i + 1], f.v[i + 2], f.v[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i += 2) *reinterpret_cast<float2 *>(p + i) = make_float2(f.v[i], f.v[i + 1]);
+  }
 }
 
 // ------------------------------------------------------------ attractive + gather
@@ -103,29 +110,51 @@ __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D>
   if (mask) pair_forces<D, U, true>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
 }
 
-// The minibatch's negatives gathered once: N (k x dim), N^T (dim x k), |n|^2, ids.
+// The minibatch's negatives gathered once: N (k x dim), N^T (dim x k), |n|^2 and
+// ids.  A CTA takes 32 consecutive negatives: warps copy their rows into N and a
+// shared tile (one row per warp step, D/32 components per lane), then every
+// thread writes one dim's 32 values of N^T as 64 contiguous bytes.
+constexpr int kGatherTile = 32;
 template <int D>
-__global__ void __launch_bounds__(kPlainWarps * 32) bf16_gather_kernel(const BF16BatchArgs a) {
-  const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) bf16_gather_kernel(const BF16BatchArgs a) {
+  constexpr int N = D / 32;  // components per lane
+  __shared__ __align__(16) __nv_bfloat16 tile[kGatherTile][D];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int epoch = a.epoch[0];
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
-  const int gw = blockIdx.x * kPlainWarps + (threadIdx.x >> 5);
-  const int gws = gridDim.x * kPlainWarps;
-  if (gw == 0 && lane == 0) *a.flag_count = 0;
-  constexpr int N = D / 32;
-  for (int k = gw; k < a.kpad; k += gws) {
+  const int k0 = blockIdx.x * kGatherTile;
+  for (int kk = warp; kk < kGatherTile; kk += 8) {
+    const int k = k0 + kk;
     int n = k < a.ns ? __ldg(negs + k) : -1;
     if (n >= a.n) n = -1;  // a draw equal to n contributes nothing
-    Frag<D> v;
-    if (n >= 0) load_bf16_row(v, a.xb + size_t(n) * D, lane);
-    else v.zero();
     float sq = 0.f;
+    if constexpr (N == 8) {
+      uint4 u = n >= 0 ? __ldg(reinterpret_cast<const uint4 *>(a.xb + size_t(n) * D) + lane) : make_uint4(0, 0, 0, 0);
+      reinterpret_cast<uint4 *>(a.nb + size_t(k) * D)[lane] = u;
+      reinterpret_cast<uint4 *>(&tile[kk][0])[lane] = u;
+      const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-    for (int t = 0; t < N; ++t) {
-      const __nv_bfloat16 h = __float2bfloat16(v.v[t]);  // exact: v came from bf16
-      a.nb[size_t(k) * D + lane * N + t] = h;
-      a.nbt[size_t(lane * N + t) * a.kpad + k] = h;
-      sq = fmaf(v.v[t], v.v[t], sq);
+      for (int i = 0; i < 4; ++i) {
+        const float lo = __uint_as_float(w[i] << 16), hi = __uint_as_float(w[i] & 0xffff0000u);
+        sq = fmaf(lo, lo, fmaf(hi, hi, sq));
+      }
+    } else if constexpr (N == 4) {
+      uint2 u = n >= 0 ? __ldg(reinterpret_cast<const uint2 *>(a.xb + size_t(n) * D) + lane) : make_uint2(0, 0);
+      reinterpret_cast<uint2 *>(a.nb + size_t(k) * D)[lane] = u;
+      reinterpret_cast<uint2 *>(&tile[kk][0])[lane] = u;
+      const uint32_t w[2] = {u.x, u.y};
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float lo = __uint_as_float(w[i] << 16), hi = __uint_as_float(w[i] & 0xffff0000u);
+        sq = fmaf(lo, lo, fmaf(hi, hi, sq));
+      }
+    } else {
+      static_assert(N == 2, "dim 64, 128 or 256");
+      uint32_t u = n >= 0 ? __ldg(reinterpret_cast<const uint32_t *>(a.xb + size_t(n) * D) + lane) : 0u;
+      reinterpret_cast<uint32_t *>(a.nb + size_t(k) * D)[lane] = u;
+      reinterpret_cast<uint32_t *>(&tile[kk][0])[lane] = u;
+      const float lo = __uint_as_float(u << 16), hi = __uint_as_float(u & 0xffff0000u);
+      sq = fmaf(lo, lo, hi * hi);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
@@ -133,6 +162,18 @@ __global__ void __launch_bounds__(kPlainWarps * 32) bf16_gather_kernel(const BF1
       a.nn[k] = sq;
       a.nid[k] = n;
     }
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < D; d += 256) {
+    uint32_t w[kGatherTile / 2];
+#pragma unroll
+    for (int i = 0; i < kGatherTile / 2; ++i) {
+      const uint32_t lo = __bfloat16_as_ushort(tile[2 * i][d]), hi = __bfloat16_as_ushort(tile[2 * i + 1][d]);
+      w[i] = lo | (hi << 16);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(a.nbt + size_t(d) * a.kpad + k0);
+#pragma unroll
+    for (int i = 0; i < kGatherTile / 8; ++i) dst[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
   }
 }
 
@@ -149,6 +190,10 @@ __global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF
   const WorkItem it = a.items[gw];
   const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
   const int cnt = it.e_end - it.e_begin;
+  if (cnt == 0) {  // a row without CSR entries: no attractive update (the update kernel reads none)
+    if (want_loss && lane == 0) a.loss_item[a.loss_off + gw] = 0.0;
+    return;
+  }
   int ids = -1;
   if (lane < cnt) {
     ids = __ldg(a.col + it.e_begin + lane);
@@ -257,10 +302,44 @@ struct RepulseSmem {
 // column half w / 4: 32 of the 64 coefficients of each chunk, and half of the
 // dims in the final update.  TMEM: S chunks in columns [0, 128) (double
 // buffered), F in columns [256, 256 + dim).
+//
+// KS = 2: the negatives of a tile are split between the two CTAs of a cluster
+// (rank 0: the first ceil(chunks / 2) chunks, rank 1 the rest), so twice as
+// many SMs work on a minibatch.  Each CTA stages its partial force
+// (its row sums) x - (its F); after a cluster barrier rank r adds the peer's
+// staged rows (read through distributed shared memory) for tile rows
+// [64 r, 64 r + 64) and stores them, and a second cluster barrier keeps both
+// CTAs' shared memory alive until the peer has read it.  Partial sums are
+// combined as own + peer, which is the same value on either rank.
 constexpr int kEpiThreads = 256;
 constexpr int kRepulseThreads = kEpiThreads + 64;
 
-template <int D>
+__device__ __forceinline__ int cta_rank_in_cluster() {
+  int r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of both CTAs arrives (release) and waits (acquire).
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t peer_addr(uint32_t local, int peer) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(peer));
+  return r;
+}
+__device__ __forceinline__ float2 ld_peer_f2(uint32_t addr) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_peer_f64(uint32_t addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+template <int D, int KS>
 __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const __grid_constant__ CUtensorMap map_x,
                                                                const __grid_constant__ CUtensorMap map_n,
                                                                const __grid_constant__ CUtensorMap map_t,
@@ -274,7 +353,12 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   __shared__ float2 negmeta[2][kChunk];  // (|n|^2, vertex id) of a chunk's negatives
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = a.kpad / kChunk;
-  const int tile_base = blockIdx.x * kTileRows;  // row offset within the minibatch
+  const int ks = KS == 2 ? cta_rank_in_cluster() : 0;
+  const int tile_base = (blockIdx.x / KS) * kTileRows;  // row offset within the minibatch
+  // this CTA's chunks [c_begin, c_end) (KS = 2 needs at least two chunks)
+  const int c_begin = ks == 0 ? 0 : (nchunks + 1) / 2;
+  const int c_end = (KS == 1 || ks == 1) ? nchunks : (nchunks + 1) / 2;
+  const int nloc = c_end - c_begin;
 
   // barrier ids
   const uint32_t b0 = smem_u32(&bar[0]);
@@ -313,6 +397,15 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   auto sN = [&](int b) { return smem_u32(sm + L::offN + b * L::kN); };
   auto sT = [&](int b) { return smem_u32(sm + L::offT + b * L::kT); };
   unsigned char *sC_ptr[2] = {sm + L::offC, sm + L::offC + L::kC};
+  // after the GEMMs: the staged force rows (pitch D + 4 floats) over the operand
+  // buffers (at dim 256 reaching into C[0]); per tile row a flag (nonzero: the
+  // row's force is final) and, with KS = 2, its loss, both in C[1]
+  constexpr int kPitch = D + 4;
+  constexpr int kPer = D / 32;  // dims per lane in the row stores
+  float *const stage = reinterpret_cast<float *>(sm + L::offN);
+  static_assert(kTileRows * kPitch * 4 <= 2 * (L::kN + L::kT) + L::kC, "staging fits before C[1]");
+  int *const row_flags = reinterpret_cast<int *>(sC_ptr[1]);
+  double *const row_loss = reinterpret_cast<double *>(sC_ptr[1] + 1024);
 
   if (warp == 8) {
     // ---------------- TMA producer
@@ -321,13 +414,13 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       mbar_expect_tx(B(FULL_X), L::kX);
       for (int ka = 0; ka < L::kAtoms; ++ka)
         tma_load_2d(sX + ka * kTileRows * 128, &map_x, ka * 64, a.base + tile_base, B(FULL_X));
-      for (int c = 0; c < nchunks && !failed(); ++c) {
-        const int b = c & 1;
-        if (c >= 2 && !mbar_wait(B(FREE_N + b), ((c >> 1) + 1) & 1, &err)) break;
+      for (int lc = 0; lc < nloc && !failed(); ++lc) {
+        const int c = c_begin + lc, b = lc & 1;
+        if (lc >= 2 && !mbar_wait(B(FREE_N + b), ((lc >> 1) + 1) & 1, &err)) break;
         mbar_expect_tx(B(FULL_N + b), L::kN);
         for (int ka = 0; ka < L::kAtoms; ++ka) tma_load_2d(sN(b) + ka * kChunk * 128, &map_n, ka * 64, c * kChunk, B(FULL_N + b));
         ++issued_n[b];
-        if (c >= 2 && !mbar_wait(B(FREE_T + b), ((c >> 1) + 1) & 1, &err)) break;
+        if (lc >= 2 && !mbar_wait(B(FREE_T + b), ((lc >> 1) + 1) & 1, &err)) break;
         mbar_expect_tx(B(FULL_T + b), L::kT);
         tma_load_2d(sT(b), &map_t, c * kChunk, 0, B(FULL_T + b));
         ++issued_t[b];
@@ -349,22 +442,22 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       constexpr uint32_t idesc2 = umma_idesc(kTileRows, D);
       const uint32_t tmem_f = tmem + 256;
       bool ok = mbar_wait(B(FULL_X), 0, &err);
-      auto gemm2 = [&](int c) {
-        const int b = c & 1;
-        if (!mbar_wait(B(C_FULL + b), (c >> 1) & 1, &err)) return false;
-        if (!mbar_wait(B(FULL_T + b), (c >> 1) & 1, &err)) return false;
+      auto gemm2 = [&](int lc) {  // lc: chunk index within this CTA's range
+        const int b = lc & 1;
+        if (!mbar_wait(B(C_FULL + b), (lc >> 1) & 1, &err)) return false;
+        if (!mbar_wait(B(FULL_T + b), (lc >> 1) & 1, &err)) return false;
         tc_fence_after();
         const uint32_t cbase = smem_u32(sC_ptr[b]);
         for (int k = 0; k < kChunk / 16; ++k)
-          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc(sT(b) + k * 32), idesc2, (c > 0 || k > 0) ? 1u : 0u);
+          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc(sT(b) + k * 32), idesc2, (lc > 0 || k > 0) ? 1u : 0u);
         umma_commit(B(C_FREE + b));
         umma_commit(B(FREE_T + b));
         return true;
       };
-      for (int c = 0; ok && c < nchunks; ++c) {
-        const int b = c & 1;
-        ok = mbar_wait(B(FULL_N + b), (c >> 1) & 1, &err);
-        if (ok && c >= 2) ok = mbar_wait(B(S_FREE + b), ((c >> 1) + 1) & 1, &err);
+      for (int lc = 0; ok && lc < nloc; ++lc) {
+        const int b = lc & 1;
+        ok = mbar_wait(B(FULL_N + b), (lc >> 1) & 1, &err);
+        if (ok && lc >= 2) ok = mbar_wait(B(S_FREE + b), ((lc >> 1) + 1) & 1, &err);
         if (!ok) break;
         tc_fence_after();
         const uint32_t tmem_s = tmem + uint32_t(b * kChunk);
@@ -374,9 +467,9 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
                  idesc1, (ka | k) ? 1u : 0u);
         umma_commit(B(FREE_N + b));
         umma_commit(B(S_FULL + b));
-        if (c >= 1) ok = gemm2(c - 1);
+        if (lc >= 1) ok = gemm2(lc - 1);
       }
-      if (ok) ok = gemm2(nchunks - 1);
+      if (ok) ok = gemm2(nloc - 1);
       umma_commit(B(F_DONE));  // also fires after a failure, once issued MMAs finish
       int dummy = 0;
       mbar_wait(B(F_DONE), 0, &dummy);  // no tensor-core work may outlive the CTA
@@ -412,30 +505,34 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     // they are idle: before chunk 1 writes C[1], and after every GEMM is done
     float *xx_part = reinterpret_cast<float *>(sC_ptr[1]);
     xx_part[hf * kTileRows + t] = xx;
-    // |n|^2 and vertex id of the chunk's negatives, staged once per chunk
+    // |n|^2 and vertex id of the chunk's negatives, staged once per chunk; this
+    // CTA's chunks start at c_begin (metadata, and the row's bitmask words)
+    const float *nn_loc = a.nn + c_begin * kChunk;
+    const int32_t *nid_loc = a.nid + c_begin * kChunk;
+    uint32_t *near_loc = a.near_bits + size_t(row_local) * kNearWords + c_begin * 2 + hf;
     const int et = hf * 128 + t;  // 0..255
-    if (et < kChunk) negmeta[0][et] = make_float2(__ldg(a.nn + et), __int_as_float(__ldg(a.nid + et)));
+    if (et < kChunk)
+      negmeta[0][et] = make_float2(__ldg(nn_loc + et), __int_as_float(__ldg(nid_loc + et)));
     epi_sync();
     xx = xx_part[t] + xx_part[kTileRows + t];
 
     float rowsum = 0.f, self_loss = 0.f;
     double loss = 0.0;
-    bool near = false;
     const float kSelfLoss = __logf(1.0f / 1e-6f);
     const uint32_t lane_base = uint32_t(q4 * 32) << 16;
-    for (int c = 0; c < nchunks; ++c) {
-      const int b = c & 1;
-      if (c > 0) epi_sync();  // meta of chunk c visible; everyone is done with chunk c-1
+    for (int lc = 0; lc < nloc; ++lc) {
+      const int b = lc & 1;
+      if (lc > 0) epi_sync();  // meta of chunk c visible; everyone is done with chunk c-1
       // next chunk's metadata: loads issued now, stored at the end of this chunk
-      const bool pre = c + 1 < nchunks && et < kChunk;
+      const bool pre = lc + 1 < nloc && et < kChunk;
       float pre_nn = 0.f;
       int pre_id = -1;
       if (pre) {
-        pre_nn = __ldg(a.nn + (c + 1) * kChunk + et);
-        pre_id = __ldg(a.nid + (c + 1) * kChunk + et);
+        pre_nn = __ldg(nn_loc + (lc + 1) * kChunk + et);
+        pre_id = __ldg(nid_loc + (lc + 1) * kChunk + et);
       }
       uint32_t s_raw[32] = {};
-      const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (c >> 1) & 1, &err));
+      const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (lc >> 1) & 1, &err));
       tc_fence_after();
       if (got) {
         tmem_ld32(tmem + lane_base + uint32_t(b * kChunk + hf * 32), s_raw);
@@ -480,11 +577,8 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         loss_c += __logf(prod);
       }
       loss += double(loss_c);
-      if (near_word) {
-        near = true;
-        a.near_bits[size_t(row_local) * kNearWords + c * 2 + hf] = near_word;
-      }
-      if (c >= 2) mbar_wait(B(C_FREE + b), ((c >> 1) + 1) & 1, &err);
+      if (near_word) near_loc[lc * 2] = near_word;
+      if (lc >= 2) mbar_wait(B(C_FREE + b), ((lc >> 1) + 1) & 1, &err);
       unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
       for (int j = 0; j < 4; ++j)
@@ -501,29 +595,17 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     loss += double(self_loss);
     float *rs_part = reinterpret_cast<float *>(sC_ptr[0]);
     double *loss_part = reinterpret_cast<double *>(sC_ptr[0] + 1024);
-    int *near_part = reinterpret_cast<int *>(sC_ptr[0] + 3072);
     rs_part[hf * kTileRows + t] = rowsum;
     loss_part[hf * kTileRows + t] = loss;
-    near_part[hf * kTileRows + t] = near ? 1 : 0;
     epi_sync();
     rowsum = rs_part[t] + rs_part[kTileRows + t];
     loss = loss_part[t] + loss_part[kTileRows + t];
-    near = (near_part[t] | near_part[kTileRows + t]) != 0;
-    if (hf == 0 && row_valid && near && done) {
-      // the pairs of near_bits are added, with the clip, by bf16_fixup_kernel
-      const int slot = atomicAdd(a.flag_count, 1);
-      a.flag_rows[slot] = row_local;
-    }
-    if (hf == 0 && row_valid && done) a.loss_row[row_global] = loss;
+    if (KS == 1 && hf == 0 && row_valid && done) a.loss_row[row_global] = loss;
     epi_sync();  // the staging below may overwrite the combine area
 
-    // Repulsive force rowsum * x - F of every tile row, staged as FP32 rows (pitch
-    // D + 4 floats) in the operand buffers, which no GEMM reads any more (at dim
-    // 256 it reaches into C[0]); x comes from the swizzled X tile.  Thread
-    // (row t, half hf) writes dims [hf D/2, (hf+1) D/2).
-    constexpr int kPitch = D + 4;
-    float *stage = reinterpret_cast<float *>(sm + L::offN);
-    static_assert(kTileRows * kPitch * 4 <= 2 * (L::kN + L::kT) + L::kC, "staging fits before C[1]");
+    // Repulsive force rowsum * x - F of every tile row, staged as FP32 rows; x
+    // comes from the swizzled X tile.  Thread (row t, half hf) writes dims
+    // [hf D/2, (hf+1) D/2).
     for (int d0 = 0; done && d0 < D / 2; d0 += 32) {
       const int dg = hf * (D / 2) + d0;  // first dim of this group of 32
       uint32_t f[32];
@@ -547,15 +629,16 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         *reinterpret_cast<float4 *>(dst + 4) = make_float4(g[4], g[5], g[6], g[7]);
       }
     }
-    int *row_flags = reinterpret_cast<int *>(sC_ptr[1]);  // nonzero: the row's force is final
-    if (hf == 0) row_flags[t] = (row_valid && done) ? (near ? 2 : 1) : 0;
+    if (hf == 0) {
+      row_flags[t] = (row_valid && done) ? 1 : 0;
+      if (KS == 2) row_loss[t] = loss;
+    }
     epi_sync();
 
     // Coalesced store of lr * force, one warp per row, each lane D/32 consecutive
     // dims, into rbuf; bf16_apply_kernel adds it to the row together with the
     // attractive update (which runs concurrently into abuf).
-    constexpr int kPer = D / 32;
-    for (int rr = warp; rr < kTileRows; rr += kEpiThreads / 32) {
+    for (int rr = warp; KS == 1 && rr < kTileRows; rr += kEpiThreads / 32) {
       if (row_flags[rr] == 0) continue;
       const int rl = tile_base + rr;
       const float *src = stage + rr * kPitch + lane * kPer;
@@ -566,6 +649,33 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         *reinterpret_cast<float2 *>(rbp + q) = make_float2(lr * f2.x, lr * f2.y);
       }
     }
+  }
+  if constexpr (KS == 2) {
+    __syncwarp();
+    cluster_barrier();  // both CTAs' staged rows, flags and losses are complete
+    if (warp < kEpiThreads / 32) {
+      const int peer = ks ^ 1;
+      const float lr = a.lr[a.epoch[0]];
+      constexpr int kHalf = kTileRows / 2;
+      for (int rr = ks * kHalf + warp; rr < (ks + 1) * kHalf; rr += kEpiThreads / 32) {
+        if (row_flags[rr] == 0) continue;
+        const float *src = stage + rr * kPitch + lane * kPer;
+        const uint32_t psrc = peer_addr(smem_u32(src), peer);
+        float *rbp = a.rbuf + size_t(tile_base + rr) * D + lane * kPer;
+#pragma unroll
+        for (int q = 0; q < kPer; q += 2) {
+          const float2 own = *reinterpret_cast<const float2 *>(src + q);
+          const float2 oth = ld_peer_f2(psrc + 4u * uint32_t(q));
+          *reinterpret_cast<float2 *>(rbp + q) = make_float2(lr * (own.x + oth.x), lr * (own.y + oth.y));
+        }
+      }
+      if (tid < kHalf) {
+        const int rr = ks * kHalf + tid;
+        if (row_flags[rr] != 0)
+          a.loss_row[a.base + tile_base + rr] = row_loss[rr] + ld_peer_f64(peer_addr(smem_u32(&row_loss[rr]), peer));
+      }
+    }
+    cluster_barrier();  // the peer has finished reading this CTA's shared memory
   }
   tc_fence_before();
   __syncthreads();
@@ -578,6 +688,36 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
 }
 
 // ------------------------------------------------------------ update
+
+// N consecutive floats through L2 (written by other kernels of this minibatch),
+// in 16-byte vectors where N allows.
+template <int N>
+__device__ __forceinline__ void ld_contig(float (&v)[N], const float *p) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < N; i += 4) {
+      const float4 t = __ldcg(reinterpret_cast<const float4 *>(p + i));
+      v[i] = t.x; v[i + 1] = t.y; v[i + 2] = t.z; v[i + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i += 2) {
+      const float2 t = __ldcg(reinterpret_cast<const float2 *>(p + i));
+      v[i] = t.x; v[i + 1] = t.y;
+    }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void st_contig(float *p, const float (&v)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < N; i += 4) *reinterpret_cast<float4 *>(p + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i += 2) *reinterpret_cast<float2 *>(p + i) = make_float2(v[i], v[i + 1]);
+  }
+}
 
 // One warp per row of the minibatch: x += abuf + rbuf (attractive and GEMM
 // repulsive updates, algo.hpp:651-666), plus, for a row with exact-path pairs
@@ -627,30 +767,35 @@ __global__ void __launch_bounds__(256) bf16_apply_kernel(const BF16BatchArgs a) 
       if (lane < kNearWords) bits_row[lane] = 0u;
       if (lane == 0) a.loss_row[row] += double(loss);
     }
-    // lane: N consecutive components, moved as float2 / bf16x2 pairs
+    // lane: N consecutive components, moved as 16-byte vectors (8-byte at dim 64)
     float *xm = a.xm + size_t(row) * D + lane * N;
     __nv_bfloat16 *xb = a.xb + size_t(row) * D + lane * N;
     const float *ab = a.abuf + size_t(row_local) * D + lane * N;
     const float *rb = a.rbuf + size_t(row_local) * D + lane * N;
-    float mv[N];
+    float mv[N], av[N], rv[N];
+    ld_contig<N>(mv, xm);
+    if (__ldg(a.rowptr + row + 1) > __ldg(a.rowptr + row)) {
+      ld_contig<N>(av, ab);
+    } else {  // no CSR entries: the attractive pass wrote nothing for this row
+#pragma unroll
+      for (int t = 0; t < N; ++t) av[t] = 0.f;
+    }
+    ld_contig<N>(rv, rb);
+#pragma unroll
+    for (int t = 0; t < N; ++t) {
+      mv[t] = mv[t] + (av[t] + rv[t]);
+      if (exact) mv[t] = mv[t] + acc.v[t];
+    }
+    st_contig<N>(xm, mv);
+    uint32_t hb[N / 2];
 #pragma unroll
     for (int t = 0; t < N; t += 2) {
-      const float2 x2 = __ldcg(reinterpret_cast<const float2 *>(xm + t));
-      const float2 a2 = __ldcg(reinterpret_cast<const float2 *>(ab + t));
-      const float2 r2 = __ldcg(reinterpret_cast<const float2 *>(rb + t));
-      mv[t] = x2.x + (a2.x + r2.x);
-      mv[t + 1] = x2.y + (a2.y + r2.y);
+      const __nv_bfloat162 h2 = __floats2bfloat162_rn(mv[t], mv[t + 1]);
+      hb[t / 2] = *reinterpret_cast<const uint32_t *>(&h2);
     }
-#pragma unroll
-    for (int t = 0; t < N; t += 2) {
-      float m0 = mv[t], m1 = mv[t + 1];
-      if (exact) {
-        m0 = m0 + acc.v[t];
-        m1 = m1 + acc.v[t + 1];
-      }
-      *reinterpret_cast<float2 *>(xm + t) = make_float2(m0, m1);
-      *reinterpret_cast<__nv_bfloat162 *>(xb + t) = __floats2bfloat162_rn(m0, m1);
-    }
+    if constexpr (N == 8) *reinterpret_cast<uint4 *>(xb) = make_uint4(hb[0], hb[1], hb[2], hb[3]);
+    else if constexpr (N == 4) *reinterpret_cast<uint2 *>(xb) = make_uint2(hb[0], hb[1]);
+    else *reinterpret_cast<uint32_t *>(xb) = hb[0];
   }
 }
 
@@ -712,42 +857,77 @@ int bf16_repulse_smem_bytes(int dim) {
   return -1;
 }
 
+namespace {
+template <int D>
+cudaError_t prepare_d() {
+  cudaError_t e = cudaFuncSetAttribute(bf16_repulse_kernel<D, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       RepulseSmem<D>::dynamic);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(bf16_repulse_kernel<D, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              RepulseSmem<D>::dynamic);
+}
+}  // namespace
+
 cudaError_t bf16_prepare(int dim) {
   switch (dim) {
-    case 64: return cudaFuncSetAttribute(bf16_repulse_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<64>::dynamic);
-    case 128: return cudaFuncSetAttribute(bf16_repulse_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<128>::dynamic);
-    case 256: return cudaFuncSetAttribute(bf16_repulse_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, RepulseSmem<256>::dynamic);
+    case 64: return prepare_d<64>();
+    case 128: return prepare_d<128>();
+    case 256: return prepare_d<256>();
   }
   return cudaErrorInvalidValue;
 }
 
 namespace {
 
+// The repulsion GEMMs of a minibatch: one CTA per 128-row tile, or, with at
+// least two chunks of negatives, a cluster of two CTAs per tile that split them.
+template <int D>
+cudaError_t launch_repulse(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
+                           const CUtensorMap &mt, int tiles, cudaStream_t s) {
+  if (a.kpad / kChunk < 2) {
+    bf16_repulse_kernel<D, 1><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s>>>(mx, mn, mt, a);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(2 * tiles);
+  cfg.blockDim = dim3(kRepulseThreads);
+  cfg.dynamicSmemBytes = RepulseSmem<D>::dynamic;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 2>, mx, mn, mt, a);
+}
+
 template <int D, int U>
 cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
                                 const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
                                 cudaEvent_t fork, cudaEvent_t join) {
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
-  const int gather_ctas = (a.kpad + kPlainWarps - 1) / kPlainWarps;  // one warp per negative
+  const int gather_ctas = a.kpad / kGatherTile;  // kpad: a multiple of 64
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
   const int apply_ctas = (a.rows + 7) / 8;
   cudaError_t e = cudaSuccess;
   if (ev || !s2) {  // one after another (per-kernel timing)
     if (ev) cudaEventRecord(ev[0], s);
-    bf16_gather_kernel<D><<<gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+    bf16_gather_kernel<D><<<gather_ctas, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
-    bf16_repulse_kernel<D><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s>>>(mx, mn, mt, a);
+    if ((e = launch_repulse<D>(a, mx, mn, mt, tiles, s)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[3], s);
     bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
     return cudaGetLastError();
   }
   // the attractive pass and the repulsion GEMMs are independent within a
   // minibatch: they run on two streams, joined before the update
-  bf16_gather_kernel<D><<<gather_ctas, kPlainWarps * 32, 0, s>>>(a);
+  bf16_gather_kernel<D><<<gather_ctas, 256, 0, s>>>(a);
   if ((e = cudaEventRecord(fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(s2, fork, 0)) != cudaSuccess) return e;
-  bf16_repulse_kernel<D><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s2>>>(mx, mn, mt, a);
+  if ((e = launch_repulse<D>(a, mx, mn, mt, tiles, s2)) != cudaSuccess) return e;
   bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
   if ((e = cudaEventRecord(join, s2)) != cudaSuccess || (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
   bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);

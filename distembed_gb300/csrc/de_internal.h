@@ -115,8 +115,6 @@ struct BF16BatchArgs {
   __nv_bfloat16 *nbt;       // [dim, kpad] the same, transposed
   float *nn;                // [kpad] squared norms of the gathered negatives
   int32_t *nid;             // [kpad] vertex id of each negative, -1 = none
-  int32_t *flag_rows;       // [B] rows with pairs that take the exact path
-  int32_t *flag_count;
   uint32_t *near_bits;      // [B, kpad / 32] bit k: pair (row, negative k) takes the exact
                             // path; zero between minibatches
   double *loss_item;        // attractive loss per work item of the epoch

@@ -100,9 +100,6 @@ struct de_handle {
   float *d_nn = nullptr;
   int32_t *d_nid = nullptr;
   size_t kpad_cap = 0;
-  int32_t *d_flag_rows = nullptr;
-  size_t flag_cap = 0;
-  int32_t *d_flag_count = nullptr;
   uint32_t *d_near_bits = nullptr;  // [B, 32], zero between minibatches
   size_t near_cap = 0;
   double *d_loss_row = nullptr;
@@ -337,8 +334,6 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.nbt = h->d_nbt;
     a.nn = h->d_nn;
     a.nid = h->d_nid;
-    a.flag_rows = h->d_flag_rows;
-    a.flag_count = h->d_flag_count;
     a.near_bits = h->d_near_bits;
     a.loss_item = h->d_loss_partial;
     a.loss_off = s.item_off[j];
@@ -373,7 +368,6 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
   int rc = DE_OK;
   if ((rc = grow(h, &h->d_abuf, &h->abuf_cap, size_t(s.batch) * h->dim, &m)) ||
       (rc = grow(h, &h->d_rbuf, &h->rbuf_cap, size_t(s.batch) * h->dim, &m)) ||
-      (rc = grow(h, &h->d_flag_rows, &h->flag_cap, size_t(s.batch), &m)) ||
       (rc = grow(h, &h->d_near_bits, &h->near_cap, size_t(s.batch) * 32, &near_moved)))
     return rc;
   if (near_moved) {
@@ -600,7 +594,6 @@ int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t 
       (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_block_sums), kFlushBlocks * sizeof(double))) != cudaSuccess ||
       (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_done), sizeof(int32_t))) != cudaSuccess ||
       (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_err), sizeof(int32_t))) != cudaSuccess ||
-      (e = dev_alloc(h, reinterpret_cast<void **>(&h->d_flag_count), sizeof(int32_t))) != cudaSuccess ||
       (e = host_alloc(h, reinterpret_cast<void **>(&h->h_epoch), 2 * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&h->upload_done, cudaEventDisableTiming)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "allocation"));
@@ -613,7 +606,6 @@ int create_handle(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t 
       (e = cudaMemsetAsync(h->d_x, 0, size_t(n) * dim * sizeof(float), st)) != cudaSuccess ||
       (e = cudaMemsetAsync(h->d_done, 0, sizeof(int32_t), st)) != cudaSuccess ||
       (e = cudaMemsetAsync(h->d_err, 0, sizeof(int32_t), st)) != cudaSuccess ||
-      (e = cudaMemsetAsync(h->d_flag_count, 0, sizeof(int32_t), st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return bail(cuda_fail(h.get(), e, "upload"));
   if (h->opt.precision == DE_PRECISION_BF16) {
@@ -660,7 +652,6 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->d_block_sums);
   dev_free(h, h->d_done);
   dev_free(h, h->d_err);
-  dev_free(h, h->d_flag_count);
   dev_free(h, h->d_xb);
   dev_free(h, h->d_abuf);
   dev_free(h, h->d_rbuf);
@@ -668,7 +659,6 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->d_nbt);
   dev_free(h, h->d_nn);
   dev_free(h, h->d_nid);
-  dev_free(h, h->d_flag_rows);
   dev_free(h, h->d_near_bits);
   dev_free(h, h->d_loss_row);
   dev_free(h, h->d_epoch);

@@ -136,7 +136,7 @@ int64_t job_bytes(const de_job_spec &s) {
   b += 8 * 2048;                                                        // small fixed buffers
   if (s.precision == DE_PRECISION_BF16) {
     const int64_t kpad = std::max<int64_t>(64, (s.ns + 63) / 64 * 64);
-    b += 2 * n * D + 8 * n + B * D * 4 + 2 * kpad * D * 2 + kpad * 8 + B * 4 + B * 32 * 4;
+    b += 2 * n * D + 8 * n + 2 * B * D * 4 + 2 * kpad * D * 2 + kpad * 8 + B * 32 * 4;  // + update rows
   }
   return b + b / 16 + (1 << 20);  // allocator rounding and slack
 }

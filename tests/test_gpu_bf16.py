@@ -47,11 +47,12 @@ def run_bf16(rp, col, x0, epochs, batch, ns, lr, quirks=True):
         return h.get_embeddings(), loss
 
 
-@pytest.mark.parametrize("dim", [64, 128, 256])
-def test_one_minibatch_gemm_path(dim):
+# negatives per minibatch -> GEMM chunks of 64: one chunk (one CTA per tile), two,
+# three (split 2 + 1 between the two CTAs of a tile's cluster) and four
+@pytest.mark.parametrize("dim,ns", [(64, 200), (128, 200), (256, 200), (128, 40), (128, 96), (256, 150)])
+def test_one_minibatch_gemm_path(dim, ns):
     n, rp, col = gg.rmat_csr(10, 8, seed=40 + dim)
     x0 = bf16_round(gg.init_embedding(n, dim, seed=1))
-    ns = 200                                    # 4 GEMM chunks after padding to 256
     prev, _ = oracle.batch_grad(rp, col, x0, n, ns, 0.02, 0, 0, n, quirks=True)
     x1, _ = run_bf16(rp, col, x0, 1, n, ns, 0.02)
     assert rel_l2(x1 - x0, prev) <= ONE_STEP_REL
