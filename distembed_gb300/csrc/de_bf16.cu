@@ -111,20 +111,20 @@ __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D>
 }
 
 // The minibatch's negatives gathered once: N (k x dim), N^T (dim x k), |n|^2 and
-// ids.  A CTA takes 32 consecutive negatives: warps copy their rows into N and a
-// shared tile (one row per warp step, D/32 components per lane), then every
-// thread writes one dim's 32 values of N^T as 64 contiguous bytes.
+// ids.  A CTA takes 32 consecutive negatives, one warp each: the warp copies its
+// row into N and a shared tile (D/32 components per lane), then thread d writes
+// dim d's 32 values of N^T as 64 contiguous bytes.
 constexpr int kGatherTile = 32;
 template <int D>
-__global__ void __launch_bounds__(256) bf16_gather_kernel(const BF16BatchArgs a) {
+__global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF16BatchArgs a) {
   constexpr int N = D / 32;  // components per lane
   __shared__ __align__(16) __nv_bfloat16 tile[kGatherTile][D];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int epoch = a.epoch[0];
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
   const int k0 = blockIdx.x * kGatherTile;
-  for (int kk = warp; kk < kGatherTile; kk += 8) {
-    const int k = k0 + kk;
+  {
+    const int kk = warp, k = k0 + kk;
     int n = k < a.ns ? __ldg(negs + k) : -1;
     if (n >= a.n) n = -1;  // a draw equal to n contributes nothing
     float sq = 0.f;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) bf16_gather_kernel(const BF16BatchArgs a)
     }
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < D; d += 256) {
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
     uint32_t w[kGatherTile / 2];
 #pragma unroll
     for (int i = 0; i < kGatherTile / 2; ++i) {
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256) bf16_gather_kernel(const BF16BatchArgs a)
 }
 
 template <int D, int U>
-__global__ void __launch_bounds__(kPlainWarps * 32) bf16_attract_kernel(const BF16BatchArgs a) {
+__global__ void __launch_bounds__(kPlainWarps * 32, 6) bf16_attract_kernel(const BF16BatchArgs a) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const bool want_loss = a.compute_loss != 0;
@@ -914,7 +914,7 @@ cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, c
   cudaError_t e = cudaSuccess;
   if (ev || !s2) {  // one after another (per-kernel timing)
     if (ev) cudaEventRecord(ev[0], s);
-    bf16_gather_kernel<D><<<gather_ctas, 256, 0, s>>>(a);
+    bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
@@ -923,10 +923,11 @@ cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, c
     bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
     return cudaGetLastError();
   }
-  // the attractive pass and the repulsion GEMMs are independent within a
-  // minibatch: they run on two streams, joined before the update
-  bf16_gather_kernel<D><<<gather_ctas, 256, 0, s>>>(a);
+  // the attractive pass and the negatives' path (gather, repulsion GEMMs) are
+  // independent within a minibatch: they run on two streams, forked after the
+  // previous minibatch's update and joined before this one's
   if ((e = cudaEventRecord(fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(s2, fork, 0)) != cudaSuccess) return e;
+  bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s2>>>(a);
   if ((e = launch_repulse<D>(a, mx, mn, mt, tiles, s2)) != cudaSuccess) return e;
   bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
   if ((e = cudaEventRecord(join, s2)) != cudaSuccess || (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
