@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
     p.add_argument("--shape", default="", help="batched form: team shape instead of the autotuner, "
-                                               "staged|rows:W:cap:steps:stages or register:vpw:W:cap")
+                                               "staged|rows:W:cap:steps:stages[:ctas] or register:vpw:W:cap")
     return p.parse_args()
 
 
@@ -500,7 +500,8 @@ def run_batched_form(args):
     if args.shape:
         f = args.shape.split(":")
         if f[0] in ("staged", "rows"):
-            b.set_shape(kernel=f[0], team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]))
+            b.set_shape(kernel=f[0], team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]),
+                        team_ctas=int(f[5]) if len(f) > 5 else 1)
         else:
             b.set_shape(kernel="register", vertices_per_warp=int(f[1]), team_warps=int(f[2]), edge_cap=int(f[3]))
         shape, tuned = b.shape(), []

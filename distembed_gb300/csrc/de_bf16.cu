@@ -203,8 +203,9 @@ __global__ void __launch_bounds__(kPlainWarps * 32, 6) bf16_attract_kernel(const
   load_bf16_row(xi, a.xb + size_t(a.base + it.row) * D, lane);
   acc.zero();
   float loss = 0.f;  // this item's loss terms (FP32); the epoch sum is FP64
-  for (int k = 0; k < cnt; k += U)
-    bf16_force_group<D, U>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
+  int k = 0;  // groups of U; a last group of at most U/2 entries runs as a group of U/2
+  for (; k + U / 2 < cnt; k += U) bf16_force_group<D, U>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
+  if (k < cnt) bf16_force_group<D, U / 2>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
 
   bool owner = true;
   if (it.nparts > 1) {

@@ -169,7 +169,7 @@ __device__ __forceinline__ void pair_forces(Frag<D> &acc, const Frag<D> &xi, con
   const float r = multi_warp_sum<U>(p, lane);
   const int v = (lane >> (5 - L)) & (U - 1);
   const bool valid = (valid_mask >> v) & 1u;
-  float c = kAttract ? -2.0f / (1.0f + r) : 2.0f / ((r + 1e-6f) * (1.0f + r));
+  float c = kAttract ? __fdividef(-2.0f, 1.0f + r) : __fdividef(2.0f, (r + 1e-6f) * (1.0f + r));
   if (!valid) c = 0.f;
   if (want_loss && valid && (lane & ((32 >> L) - 1)) == 0)
     loss += kAttract ? log1pf(r) : logf((1.0f + r) / (r + 1e-6f));

@@ -70,13 +70,16 @@ __device__ __forceinline__ void force_group(const PlainBatchArgs &a, Frag<D> &ac
   if (mask) pair_forces<D, U, kAttract>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
 }
 
-// Forces of the ids held by the warp's lanes (-1 = none), U at a time.
+// Forces of the ids held by the warp's lanes (-1 = none), U at a time; a last
+// group of at most U/2 entries runs as a group of U/2.
 template <int D, int U, bool kAttract, bool kAfterWait>
 __device__ __forceinline__ void force_lanes(const PlainBatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
                                             int cnt, float lr, float bound, bool want_loss, float &loss,
                                             int lane) {
-  for (int k = 0; k < cnt; k += U)
+  int k = 0;
+  for (; k + U / 2 < cnt; k += U)
     force_group<D, U, kAttract, kAfterWait>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
+  if (k < cnt) force_group<D, U / 2, kAttract, kAfterWait>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
 }
 
 template <int D, int U>
