@@ -678,7 +678,7 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
   for (int v : {1, 2, 4})
     for (int w : {4, 8, 16, 32})
       for (int c : {32, 64, 128}) cand.push_back(de_batch_shape{DE_BATCH_REGISTER, v, w, c, 0, 0, 1});
-  if (ns <= kStagedMaxNs)
+  if (ns <= kStagedMaxNs) {  // the staged kernels take at most 32 negatives
     for (int fam : {DE_BATCH_STAGED, DE_BATCH_ROWS})
       for (int w : {4, 8, 12, 16})
         for (int c : {8, 16, 32})
@@ -688,6 +688,7 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
       for (int c : {16, 32})
         for (int u : {1, 2})
           for (int st : {3, 4}) cand.push_back(de_batch_shape{DE_BATCH_STAGED, 0, w, c, u, st, 2});
+  }
   const bool bf16 = b->opt.precision == DE_PRECISION_BF16;
   std::vector<double> lrs(epochs, lr);
   float best_ms = -1.f;

@@ -173,6 +173,17 @@ def test_autotune_keeps_embeddings_and_picks_a_valid_shape():
         assert np.array_equal(got[i], xs[i]) and np.array_equal(loss[i], ls[i])
 
 
+def test_autotune_with_more_negatives_than_the_staged_kernels_take():
+    # ns > 32: only the register kernel's shapes are timed
+    dim, B, ns = 32, 128, 40
+    graphs = GRAPHS[:3]
+    with de.Batch([(rp, c) for _, _, rp, c in graphs], dim) as b:
+        for i, (_, n, _, _) in enumerate(graphs):
+            b.set_embeddings(i, x_init(i, n, dim))
+        best, tried = b.autotune(1, B, ns, 0.02)
+        assert tried and {sh["kernel"] for sh, _ in tried} == {0} and best["kernel"] == 0
+
+
 def test_edge_updates_is_the_sum_over_graphs():
     dim, E, B, ns = 32, 3, 256, 5
     with de.Batch([(rp, c) for _, _, rp, c in GRAPHS], dim) as b:
