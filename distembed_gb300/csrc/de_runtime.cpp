@@ -775,10 +775,12 @@ static int prepare_run(de_handle *h, int32_t first_epoch, int32_t epochs, int32_
   for (int i = 0; i < epochs; ++i) h->h_lr[i] = float(lr_per_epoch[i]);
   DE_CUDA(h, cudaMemcpyAsync(h->d_negs, h->h_negs, nneg * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   DE_CUDA(h, cudaMemcpyAsync(h->d_lr, h->h_lr, epochs * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-  DE_CUDA(h, cudaEventRecord(h->upload_done, h->stream));
   h->h_epoch[0] = 0;
   h->h_epoch[1] = first_epoch;
   DE_CUDA(h, cudaMemcpyAsync(h->d_epoch, h->h_epoch, 2 * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  // after every copy from the pinned buffers: the next call waits on it before
+  // writing them again
+  DE_CUDA(h, cudaEventRecord(h->upload_done, h->stream));
   return DE_OK;
 }
 
