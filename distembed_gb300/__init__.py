@@ -38,7 +38,8 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
            "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
            "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error",
-           "de_mm_read", "de_embedding_write")
+           "de_mm_read", "de_embedding_write", "de_mm_read_gpu", "de_coo_to_csr", "de_csr_info", "de_csr_copy",
+           "de_csr_free")
 
 
 class BatchShape(ctypes.Structure):
@@ -161,6 +162,12 @@ def lib():
         L.de_server_last_error.restype = ctypes.c_char_p
         L.de_mm_read.argtypes = [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _i64]
         L.de_embedding_write.argtypes = [ctypes.c_char_p, _vp, _i64, _i32]
+        L.de_mm_read_gpu.argtypes = [ctypes.c_char_p, _i32, _vp]
+        L.de_coo_to_csr.argtypes = [_i64, _i64, _vp, _vp, _i64, _i32, _i32, _vp]
+        L.de_csr_info.argtypes = [_vp, _vp, _vp, _vp]
+        L.de_csr_copy.argtypes = [_vp, _vp, _vp]
+        L.de_csr_free.argtypes = [_vp]
+        L.de_csr_free.restype = None
         _lib = L
     return _lib
 
@@ -174,10 +181,40 @@ def _ptr(a) -> int:
 DRIVER_PATH = os.path.join(HERE, "dist_embed_gb300")
 
 
-def read_mtx(path: str):
-    """MatrixMarket -> (rows, cols, rowptr, col) int64 CSR, by the library's
-    reader (cpp/io/parrallel_IO.hpp:31-88 semantics at one rank)."""
+def _take_csr(L, rc, h):
+    if rc != DE_OK:
+        raise DEError(rc, L.de_last_error(None).decode())
+    try:
+        r, c, z = _i64(0), _i64(0), _i64(0)
+        L.de_csr_info(h, ctypes.byref(r), ctypes.byref(c), ctypes.byref(z))
+        rowptr = np.zeros(r.value + 1, dtype=np.int64)
+        col = np.zeros(max(z.value, 1), dtype=np.int64)
+        L.de_csr_copy(h, rowptr.ctypes.data, col.ctypes.data)
+        return r.value, c.value, rowptr, col[: z.value]
+    finally:
+        L.de_csr_free(h)
+
+
+def coo_to_csr(rows: int, cols: int, row_idx, col_idx, mirror: bool = False, device: int = 0):
+    """COO -> (rows, cols, rowptr, col) int64 CSR on the GPU: duplicates merged,
+    columns ascending, mirrored off-diagonal entries added when mirror."""
     L = lib()
+    ri = np.ascontiguousarray(row_idx, dtype=np.int64)
+    ci = np.ascontiguousarray(col_idx, dtype=np.int64)
+    h = _vp()
+    rc = L.de_coo_to_csr(rows, cols, ri.ctypes.data, ci.ctypes.data, len(ri), int(mirror), device, ctypes.byref(h))
+    return _take_csr(L, rc, h)
+
+
+def read_mtx(path: str, gpu: bool = False, device: int = 0):
+    """MatrixMarket -> (rows, cols, rowptr, col) int64 CSR, by the library's
+    reader (cpp/io/parrallel_IO.hpp:31-88 semantics at one rank); gpu: the
+    COO -> CSR on GPU `device`."""
+    L = lib()
+    if gpu:
+        h = _vp()
+        rc = L.de_mm_read_gpu(path.encode(), device, ctypes.byref(h))
+        return _take_csr(L, rc, h)
     r, c, z = _i64(0), _i64(0), _i64(0)
     rc = L.de_mm_read(path.encode(), ctypes.byref(r), ctypes.byref(c), ctypes.byref(z), None, None, 0)
     if rc != DE_OK:

@@ -299,7 +299,7 @@ double de_server_clock(const de_server *s);
 int de_server_destroy(de_server *s);
 const char *de_server_last_error(const de_server *s);
 
-/* ---- Input and output of the driver (host only, no GPU needed).
+/* ---- Input and output of the driver (de_mm_read and the writer: host only).
  * MatrixMarket reader with the semantics of ParallelIO::parallel_read_MM
  * (cpp/io/parrallel_IO.hpp:31-88) at one rank: coordinate format, 1-based,
  * duplicates merged, values ignored, a symmetric header mirrors off-diagonal
@@ -307,6 +307,22 @@ const char *de_server_last_error(const de_server *s);
  * (rows, cols, nnz after merging), then with rowptr[rows+1], col[capacity >= nnz]. */
 int de_mm_read(const char *path, int64_t *rows, int64_t *cols, int64_t *nnz, int64_t *rowptr, int64_t *col,
                int64_t capacity);
+/* The same reader with the COO -> CSR (sort of the entries, merge of duplicates,
+ * row pointers) on GPU `device`: the file is parsed on the host once, the CSR is
+ * the one de_mm_read returns.  The result is read through de_csr_info /
+ * de_csr_copy and released with de_csr_free. */
+typedef struct de_csr de_csr;
+int de_mm_read_gpu(const char *path, int32_t device, de_csr **out);
+/* COO -> CSR on GPU `device` for 0-based entries (row_idx[e], col_idx[e]) of a
+ * rows x cols matrix, with the mirrored entry of every off-diagonal one when
+ * mirror != 0; duplicates merged, columns ascending within a row
+ * (cpp/core/csr_local.hpp:37-125 at one rank, MKL's order defined as ascending). */
+int de_coo_to_csr(int64_t rows, int64_t cols, const int64_t *row_idx, const int64_t *col_idx, int64_t nnz,
+                  int32_t mirror, int32_t device, de_csr **out);
+int de_csr_info(const de_csr *c, int64_t *rows, int64_t *cols, int64_t *nnz);
+/* rowptr[rows + 1], col[nnz]. */
+int de_csr_copy(const de_csr *c, int64_t *rowptr, int64_t *col);
+void de_csr_free(de_csr *c);
 /* Embedding writer of ParallelIO::parallel_write (cpp/io/parrallel_IO.hpp:90-146):
  * per row "%lu" (1-based id), dim times " %.5f", "\n"; no header. */
 int de_embedding_write(const char *path, const double *x, int64_t rows, int32_t dim);

@@ -99,3 +99,52 @@ void f(SpMat *s, DenseMat *d, Grid *g) {
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def _big_file(path, n, m, seed, bad_at=None, extra=0):
+    """A general file of m random entries over n vertices, comment lines every
+    1000 entries, optionally a malformed entry line at index bad_at and `extra`
+    entries past the declared count."""
+    rng = np.random.default_rng(seed)
+    r, c = rng.integers(1, n + 1, m + extra), rng.integers(1, n + 1, m + extra)
+    with open(path, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate real general\n% generated\n")
+        f.write(f"{n} {n} {m}\n")
+        for e in range(m + extra):
+            if e % 1000 == 0:
+                f.write("% a comment between entries\n")
+            if e == bad_at:
+                f.write(f"{r[e]} x\n")
+            else:
+                f.write(f"  {r[e]}\t{c[e]} 0.5\n")
+    return r[:m] - 1, c[:m] - 1
+
+
+def test_reader_large_file_in_chunks(tmp_path):
+    # a file of several MB is parsed by several host threads; entries past the
+    # declared count are not read (as the one-line-at-a-time reference reader)
+    p = str(tmp_path / "big.mtx")
+    r, c = _big_file(p, 5000, 200000, 3, extra=500)
+    rows, cols, rp, col = de.read_mtx(p)
+    key = np.unique(r * 5000 + c)
+    want_rp = np.zeros(5001, np.int64)
+    np.add.at(want_rp, key // 5000 + 1, 1)
+    assert rows == cols == 5000
+    assert np.array_equal(rp, np.cumsum(want_rp)) and np.array_equal(col, key % 5000)
+
+
+def test_reader_reports_the_first_bad_entry_by_number(tmp_path):
+    p = str(tmp_path / "bad.mtx")
+    _big_file(p, 5000, 200000, 4, bad_at=171234)
+    with pytest.raises(de.DEError, match="bad MatrixMarket entry 171235"):
+        de.read_mtx(p)
+    # a malformed line after the declared entries is never read
+    q = str(tmp_path / "late.mtx")
+    _big_file(q, 5000, 200000, 4, bad_at=200100, extra=200)
+    assert de.read_mtx(q)[0] == 5000
+    # fewer entries than declared
+    t = str(tmp_path / "short.mtx")
+    with open(t, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate pattern general\n3 3 4\n1 2\n2 3\n")
+    with pytest.raises(de.DEError, match="ends early"):
+        de.read_mtx(t)
