@@ -39,7 +39,7 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
            "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error",
            "de_mm_read", "de_embedding_write", "de_mm_read_gpu", "de_coo_to_csr", "de_csr_info", "de_csr_copy",
-           "de_csr_free")
+           "de_csr_free", "de_spmm", "de_spmm_f32")
 
 
 class BatchShape(ctypes.Structure):
@@ -163,6 +163,8 @@ def lib():
         L.de_mm_read.argtypes = [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _i64]
         L.de_embedding_write.argtypes = [ctypes.c_char_p, _vp, _i64, _i32]
         L.de_mm_read_gpu.argtypes = [ctypes.c_char_p, _i32, _vp]
+        L.de_spmm.argtypes = [_vp, _i32, ctypes.c_double, _vp]
+        L.de_spmm_f32.argtypes = [_vp, _i32, ctypes.c_float, _vp, _i32]
         L.de_coo_to_csr.argtypes = [_i64, _i64, _vp, _vp, _i64, _i32, _i32, _vp]
         L.de_csr_info.argtypes = [_vp, _vp, _vp, _vp]
         L.de_csr_copy.argtypes = [_vp, _vp, _vp]
@@ -331,6 +333,20 @@ class Handle:
 
     def edge_updates(self, epochs: int, batch_size: int, ns: int, first_epoch: int = 0) -> int:
         return int(lib().de_edge_updates(self._h, first_epoch, epochs, batch_size, ns))
+
+    def spmm(self, batch_size: int, lr: float, out=None, dtype=np.float64):
+        """The reference's SpMM step (cpp/algo/spmm.hpp:54-159): y = lr * A x from
+        the current embedding x, which does not change.  out: host FP64 or FP32
+        array, or a CUDA FP32 tensor."""
+        if out is None:
+            out = np.empty((self.n, self.dim), dtype=dtype)
+        if hasattr(out, "is_cuda") and out.is_cuda:
+            self._check(lib().de_spmm_f32(self._h, batch_size, lr, out.data_ptr(), 1))
+        elif str(out.dtype) in ("float32", "torch.float32"):
+            self._check(lib().de_spmm_f32(self._h, batch_size, lr, _ptr(out), 0))
+        else:
+            self._check(lib().de_spmm(self._h, batch_size, lr, out.ctypes.data))
+        return out
 
     def close(self):
         if getattr(self, "_h", None):

@@ -31,7 +31,7 @@ struct WorkItem {
   int32_t first_slot;  // split rows: first slot of the row
   int32_t part;        // split rows: index of this part
   int32_t counter;     // split rows: first counter of the row
-  int32_t pad;
+  int32_t batch;       // minibatch of the item (the one-launch SpMM)
 };
 static_assert(sizeof(WorkItem) == 32, "WorkItem layout");
 
@@ -91,6 +91,22 @@ struct FlushArgs {
 };
 
 constexpr int kFlushBlocks = 152;
+
+// The SpMM step (spmm_kernel): every work item of every minibatch in one launch,
+// y rows from the unchanged input x; a minibatch's split rows use partial slots
+// from slot_off[j] and counters from counter_off[j] (WorkItem::batch = j).
+struct SpmmArgs {
+  const float *X;
+  float *Y;
+  const int32_t *col;
+  const WorkItem *items;
+  int64_t n_items;
+  int32_t batch, skip;
+  const int32_t *slot_off, *counter_off;
+  float lr;
+  float *P;
+  int32_t *counters;
+};
 
 // Kernel arguments of one minibatch of the BF16 precision form.
 struct BF16BatchArgs {
@@ -168,6 +184,7 @@ int copy_loss(de_handle *h, double *out, int32_t epochs);
 // previous kernel in the stream.
 cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool pdl, cudaStream_t s);
 cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s);
+cudaError_t launch_spmm(int dim, const SpmmArgs &a, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
 constexpr int kPlainWarps = 4;      // warps per CTA of the plain batch kernel

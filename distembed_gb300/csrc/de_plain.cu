@@ -184,6 +184,64 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
   }
 }
 
+// SpMMAlgo::algo_spmm's step at one rank (cpp/algo/spmm.hpp:54-159):
+// y[i] = sum over the CSR entries of row i, in CSR order, of lr * x[col]
+// (spmm.hpp:358-392), from the unchanged input x into the output y
+// (spmm.hpp:397-412).  The reference goes minibatch by minibatch; the rows do not
+// depend on one another, so every work item runs in one launch.  One warp per
+// work item, U rows in flight; split rows are combined in piece order as in
+// plain_batch_kernel.
+template <int D, int U>
+__global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBlocks)
+    spmm_kernel(const SpmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = blockIdx.x * int64_t(kPlainWarps) + (threadIdx.x >> 5);
+  if (gw >= a.n_items) return;
+  const WorkItem it = a.items[gw];
+  const int j = it.batch;
+  float *const P = a.P + size_t(__ldg(a.slot_off + j)) * D;
+  int32_t *const counters = a.counters + __ldg(a.counter_off + j);
+  const int cnt = it.e_end - it.e_begin;
+  int ids = -1;
+  if (lane < cnt) {
+    ids = __ldg(a.col + it.e_begin + lane);
+    if (ids == a.skip) ids = -1;  // edges into n-1 (spmm.hpp:260-265, 365)
+  }
+  Frag<D> acc;
+  acc.zero();
+  for (int k = 0; k < cnt; k += U) {
+    Frag<D> xn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int n = __shfl_sync(kFull, ids, (k + u) & 31);
+      if (k + u < cnt && n >= 0) load_nc(xn[u], a.X + size_t(n) * D, lane);
+      else xn[u].zero();
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int t = 0; t < Frag<D>::N; ++t) acc.v[t] = fmaf(a.lr, xn[u].v[t], acc.v[t]);
+  }
+  bool owner = true;
+  if (it.nparts > 1) {
+    const int NP = it.nparts;
+    const int g = it.part / kCombineGroup;
+    const int ng = (NP + kCombineGroup - 1) / kCombineGroup;
+    const int gsize = min(kCombineGroup, NP - g * kCombineGroup);
+    store<D, true>(acc, P + size_t(it.first_slot + it.part) * D, lane);
+    owner = arrive_last(counters + it.counter + g, gsize, lane);
+    if (owner) {
+      sum_slots(acc, P + size_t(it.first_slot + g * kCombineGroup) * D, gsize, lane);
+      if (ng > 1) {
+        store<D, true>(acc, P + size_t(it.first_slot + NP + g) * D, lane);
+        owner = arrive_last(counters + it.counter + ng, ng, lane);
+        if (owner) sum_slots(acc, P + size_t(it.first_slot + NP) * D, ng, lane);
+      }
+    }
+  }
+  if (owner) store<D, false>(acc, a.Y + (size_t(j) * a.batch + it.row) * D, lane);
+}
+
 // End of an epoch: write back the last minibatch, reduce the epoch's loss
 // partials in a fixed order (each CTA a fixed chunk, then the last CTA to
 // finish sums the chunk sums in order), advance the epoch counter.
@@ -272,6 +330,20 @@ cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool 
     case 256: return launch(plain_batch_kernel<256, 4>, grid, block, a, pdl, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_spmm(int dim, const SpmmArgs &a, cudaStream_t s) {
+  const int64_t grid = (a.n_items + kPlainWarps - 1) / kPlainWarps;
+  if (grid == 0) return cudaSuccess;
+  if (grid >= (int64_t(1) << 31)) return cudaErrorInvalidValue;
+  switch (dim) {
+    case 32: spmm_kernel<32, 8><<<unsigned(grid), kPlainWarps * 32, 0, s>>>(a); break;
+    case 64: spmm_kernel<64, 8><<<unsigned(grid), kPlainWarps * 32, 0, s>>>(a); break;
+    case 128: spmm_kernel<128, 8><<<unsigned(grid), kPlainWarps * 32, 0, s>>>(a); break;
+    case 256: spmm_kernel<256, 4><<<unsigned(grid), kPlainWarps * 32, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s) {

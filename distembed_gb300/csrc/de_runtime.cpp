@@ -51,6 +51,10 @@ struct de_handle {
   // per-minibatch-size state
   Schedule sched;
   float *d_stage = nullptr;  // three minibatch staging buffers
+  float *d_y = nullptr;      // SpMM output [n, dim]
+  int32_t *d_spmm_off = nullptr;  // SpMM: per-minibatch first partial slot, then first counter
+  int spmm_batch = 0, spmm_cap = 0;
+  int64_t spmm_parts = 0, spmm_split = 0;
   size_t stage_cap = 0;
   float *d_parts = nullptr;
   size_t parts_cap = 0;
@@ -217,13 +221,13 @@ void build_schedule(const de_handle *h, int B, int cap, Schedule &s, std::vector
       const int64_t e0 = h->rowptr[base + r], e1 = h->rowptr[base + r + 1];
       const int64_t deg = e1 - e0;
       if (deg <= cap) {
-        items.push_back(WorkItem{r, int32_t(e0), int32_t(e1), 1, 0, 0, 0, 0});
+        items.push_back(WorkItem{r, int32_t(e0), int32_t(e1), 1, 0, 0, 0, j});
       } else {
         const int np = int((deg + cap - 1) / cap);
         const int ng = (np + kCombineGroup - 1) / kCombineGroup;
         for (int p = 0; p < np; ++p) {
           const int64_t a = e0 + int64_t(p) * cap, b = std::min<int64_t>(e1, a + cap);
-          items.push_back(WorkItem{r, int32_t(a), int32_t(b), np, parts, p, split, 0});
+          items.push_back(WorkItem{r, int32_t(a), int32_t(b), np, parts, p, split, j});
         }
         parts += np + (ng > 1 ? ng : 0);
         split += ng + (ng > 1 ? 1 : 0);
@@ -646,6 +650,8 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->d_x);
   dev_free(h, h->sched.d_items);
   dev_free(h, h->d_stage);
+  dev_free(h, h->d_y);
+  dev_free(h, h->d_spmm_off);
   dev_free(h, h->d_parts);
   dev_free(h, h->d_counters);
   dev_free(h, h->d_loss_partial);
@@ -682,9 +688,10 @@ int de_destroy(de_handle *h) {
   return DE_OK;
 }
 
-static int copy_embeddings_f64(de_handle *h, double *host, bool to_device) {
+static int copy_embeddings_f64(de_handle *h, double *host, bool to_device, float *dev = nullptr) {
   if (!h || !host) return fail(h, DE_ERR_INVALID, "NULL argument");
   DE_CUDA(h, cudaSetDevice(h->device));
+  if (!dev) dev = h->d_x;
   const int64_t total = h->n * h->dim;
   const int64_t chunk = std::min<int64_t>(total, int64_t(8) << 20);  // 64 MiB of FP64
   if (int rc = grow(h, &h->d_stage64, &h->stage64_cap, size_t(chunk))) return rc;
@@ -692,10 +699,10 @@ static int copy_embeddings_f64(de_handle *h, double *host, bool to_device) {
     const int64_t cnt = std::min(chunk, total - off);
     if (to_device) {
       DE_CUDA(h, cudaMemcpyAsync(h->d_stage64, host + off, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-      DE_CUDA(h, launch_f64_to_f32(h->d_stage64, h->d_x + off, cnt, h->stream));
-      if (h->d_xb) DE_CUDA(h, launch_f32_to_bf16(h->d_x + off, h->d_xb + off, cnt, h->stream));
+      DE_CUDA(h, launch_f64_to_f32(h->d_stage64, dev + off, cnt, h->stream));
+      if (h->d_xb) DE_CUDA(h, launch_f32_to_bf16(dev + off, h->d_xb + off, cnt, h->stream));
     } else {
-      DE_CUDA(h, launch_f32_to_f64(h->d_x + off, h->d_stage64, cnt, h->stream));
+      DE_CUDA(h, launch_f32_to_f64(dev + off, h->d_stage64, cnt, h->stream));
       DE_CUDA(h, cudaMemcpyAsync(host + off, h->d_stage64, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     }
   }
@@ -806,6 +813,72 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
     if ((rc = check_device_error(h))) return rc;
   }
   DE_CUDA(h, cudaGetLastError());
+  return DE_OK;
+}
+
+// SpMMAlgo::algo_spmm(1, batch_size, lr) at one rank (cpp/algo/spmm.hpp:54-159):
+// the rows of each minibatch into d_y from the current embedding.
+static int spmm_run(de_handle *h, int32_t batch_size, double lr) {
+  if (batch_size <= 0) return fail(h, DE_ERR_INVALID, "batch_size > 0");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  if (int rc = ensure_schedule(h, batch_size)) return rc;
+  const Schedule &s = h->sched;
+  // the minibatches do not depend on one another: every item in one launch, each
+  // minibatch with its own partial slots and counters
+  if (h->spmm_batch != s.batch || h->spmm_cap != s.edge_cap) {
+    std::vector<int32_t> off(2 * size_t(s.batches) + 2, 0);
+    for (int j = 0; j < s.batches; ++j) {
+      off[j + 1] = off[j] + s.n_parts[j];
+      off[s.batches + 1 + j + 1] = off[s.batches + 1 + j] + s.n_split[j];
+    }
+    h->spmm_parts = off[s.batches];
+    h->spmm_split = off[2 * size_t(s.batches) + 1];
+    if (h->d_spmm_off) dev_free(h, h->d_spmm_off);
+    h->d_spmm_off = nullptr;
+    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_spmm_off), off.size() * sizeof(int32_t)));
+    DE_CUDA(h, cudaMemcpyAsync(h->d_spmm_off, off.data(), off.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               h->stream));
+    DE_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->spmm_batch = s.batch;
+    h->spmm_cap = s.edge_cap;
+  }
+  bool moved = false, counters_moved = false;
+  int rc = DE_OK;
+  if ((rc = grow(h, &h->d_parts, &h->parts_cap, size_t(std::max<int64_t>(h->spmm_parts, 1)) * h->dim, &moved)) ||
+      (rc = grow(h, &h->d_counters, &h->counters_cap, size_t(std::max<int64_t>(h->spmm_split, 1)), &counters_moved)))
+    return rc;
+  if (counters_moved) DE_CUDA(h, cudaMemsetAsync(h->d_counters, 0, h->counters_cap * sizeof(int32_t), h->stream));
+  if (moved || counters_moved) drop_graph(h);
+  if (!h->d_y) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_y), size_t(h->n) * h->dim * sizeof(float)));
+  SpmmArgs a{};
+  a.X = h->d_x;
+  a.Y = h->d_y;
+  a.col = h->d_col;
+  a.items = s.d_items;
+  a.n_items = s.n_items;
+  a.batch = s.batch;
+  a.slot_off = h->d_spmm_off;
+  a.counter_off = h->d_spmm_off + s.batches + 1;
+  a.skip = h->opt.ref_quirks ? int32_t(h->n - 1) : -1;
+  a.lr = float(lr);
+  a.P = h->d_parts;
+  a.counters = h->d_counters;
+  DE_CUDA(h, launch_spmm(h->dim, a, h->stream));
+  return DE_OK;
+}
+
+int de_spmm(de_handle *h, int32_t batch_size, double lr, double *y) {
+  if (!h || !y) return DE_ERR_INVALID;
+  if (int rc = spmm_run(h, batch_size, lr)) return rc;
+  return copy_embeddings_f64(h, y, false, h->d_y);
+}
+
+int de_spmm_f32(de_handle *h, int32_t batch_size, float lr, float *y, int32_t on_device) {
+  if (!h || !y) return DE_ERR_INVALID;
+  if (int rc = spmm_run(h, batch_size, lr)) return rc;
+  DE_CUDA(h, cudaMemcpyAsync(y, h->d_y, size_t(h->n) * h->dim * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
   return DE_OK;
 }
 

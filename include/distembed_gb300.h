@@ -327,6 +327,16 @@ void de_csr_free(de_csr *c);
  * per row "%lu" (1-based id), dim times " %.5f", "\n"; no header. */
 int de_embedding_write(const char *path, const double *x, int64_t rows, int32_t dim);
 
+/* SpMMAlgo::algo_spmm(1, batch_size, lr) at one rank (cpp/algo/spmm.hpp:54-159),
+ * as BaselineSpMM::execute runs it for -spmm 1 (cpp/algo/baseline_spmm.hpp:63-88):
+ * y = lr * A x for the handle's CSR and current embedding x, minibatch by
+ * minibatch (the rows do not depend on one another; x is not changed); with
+ * ref_quirks edges into vertex n-1 are skipped (spmm.hpp:260-265, 365).
+ * y: host FP64 n x dim (the output DenseMat's layout). */
+int de_spmm(de_handle *h, int32_t batch_size, double lr, double *y);
+/* The same into an FP32 n x dim buffer (a device pointer when on_device). */
+int de_spmm_f32(de_handle *h, int32_t batch_size, float lr, float *y, int32_t on_device);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 

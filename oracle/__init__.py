@@ -53,6 +53,8 @@ def lib():
                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int]
         L.oracle_run_batches.restype = ctypes.c_int64
+        L.oracle_spmm.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_double, ctypes.c_int,
+                                  _f64p]
         _LIB = L
     return _LIB
 
@@ -78,6 +80,8 @@ def ref():
         L.deref_negatives.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.POINTER(ctypes.c_uint64)]
         L.deref_csr.argtypes = [ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _i64p, _i64p]
+        L.deref_spmm.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p, ctypes.c_int,
+                                 ctypes.c_double, _f64p]
         _REF = L
     return _REF
 
@@ -126,6 +130,18 @@ def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0):
     return x, loss[:epochs]
 
 
+def spmm(rowptr, col, x, lr, quirks=True):
+    """The reference's SpMM step (cpp/algo/spmm.hpp:54-159): y = lr * A x, FP64."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, dim = x.shape
+    y = np.zeros((n, dim), dtype=np.float64)
+    rc = lib().oracle_spmm(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), lr, int(quirks), _p(y, _f64p))
+    if rc != 0:
+        raise ValueError(f"oracle_spmm failed ({rc})")
+    return y
+
+
 def run_batches(rowptr, col, x, epoch_in_call, batch, ns, lr, batch_ids, quirks=True, threads=0):
     """Runs the listed minibatches of one epoch in place on x (FP64, C-contiguous);
     returns the edge-updates performed.  Used for bounded CPU timing samples."""
@@ -161,6 +177,19 @@ def ref_run(rowptr, col, x, epochs, batch, ns, lr, driver_loop=False):
     if rc != 0:
         raise ValueError(f"deref_run failed ({rc})")
     return x
+
+
+def ref_spmm(rowptr, col, x, batch, lr):
+    """The reference's own SpMMAlgo::algo_spmm(1, batch, lr) (FP64): y."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, dim = x.shape
+    y = np.zeros((n, dim), dtype=np.float64)
+    rc = ref().deref_spmm(dim, n, len(col), _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), batch, lr,
+                          _p(y, _f64p))
+    if rc != 0:
+        raise ValueError(f"deref_spmm failed ({rc})")
+    return y
 
 
 def ref_batch_grad(rowptr, col, x, batch, ns, lr, batch_id, seed, considering):

@@ -24,6 +24,7 @@
  *   F9  a negative draw equal to n (the sampler's upper bound is inclusive) makes
  *       the reference index a one-element vector out of range (algo.hpp:605-617).
  *       Such draws contribute nothing here, in both modes.
+ * Also: the reference's SpMM step (oracle_spmm, cpp/algo/spmm.hpp:54-159, 358-412).
  * The loss (absent from the reference) is the t-distribution objective whose
  * negative gradient is the force before clipping:
  *   attractive pair  log(1 + r)
@@ -237,6 +238,30 @@ int64_t oracle_run_batches(int64_t n, const int64_t *rowptr, const int64_t *col,
     updates += int64_t(rep_rows) * valid;
   }
   return updates;
+}
+
+/* SpMMAlgo::algo_spmm at one rank (cpp/algo/spmm.hpp:54-159): for every row i,
+ * y[i] = sum over the CSR entries e of row i, in CSR order, of lr * x[col[e]]
+ * (spmm.hpp:358-392, accumulated from zero as prevCoordinates, spmm.hpp:116-121,
+ * then stored into the output matrix, spmm.hpp:397-412).  x is not changed; the
+ * minibatch size only orders the rows, which do not depend on one another.  With
+ * quirks, edges into vertex n-1 are skipped (the destination filter
+ * `dst_id < dst_end_index`, dst_end_index = gCols - 1, spmm.hpp:260-265, 365). */
+int oracle_spmm(int64_t n, const int64_t *rowptr, const int64_t *col, int dim, const double *x, double lr,
+                int quirks, double *y) {
+  const int64_t skip = quirks ? n - 1 : -1;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    double *yi = y + i * dim;
+    for (int d = 0; d < dim; ++d) yi[d] = 0.0;
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      const int64_t c = col[e];
+      if (c == skip) continue;
+      const double *xc = x + c * dim;
+      for (int d = 0; d < dim; ++d) yi[d] = yi[d] + lr * xc[d];
+    }
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -1,8 +1,9 @@
 /*
  * TEST INFRASTRUCTURE ONLY — never linked into the product.
  *
- * Drives the reference's own embedding step, compiled unmodified from its
- * sources (cpp/algo/algo.hpp, cpp/core/common.cpp, cpp/net/process_3D_grid.cpp)
+ * Drives the reference's own embedding step and SpMM step, compiled unmodified
+ * from their sources (cpp/algo/algo.hpp, cpp/algo/spmm.hpp, cpp/core/common.cpp,
+ * cpp/net/process_3D_grid.cpp)
  * against the single-rank stand-ins in oracle/shim/.  It exposes a small C ABI
  * used to (1) pin the FP64 restatement in oracle/de_oracle.cpp bit-for-bit and
  * (2) write the golden vectors under tests/golden/.
@@ -15,6 +16,7 @@
  * alpha 0, beta 0.25, bounds +-5, row-major, async comm (the driver defaults).
  */
 #include "algo/algo.hpp"
+#include "algo/spmm.hpp"
 
 #include <cstring>
 #include <memory>
@@ -130,9 +132,39 @@ int grad_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col,
   return 0;
 }
 
+template <size_t D>
+int spmm_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, const double *x, int batch,
+             double lr, double *y) {
+  RefGraph g(n, nnz, rowptr, col, batch);
+  DenseMat<INDEX_TYPE, double, D> dense(&g.grid, INDEX_TYPE(n)), out(&g.grid, INDEX_TYPE(n));
+  std::memcpy(dense.nCoordinates, x, sizeof(double) * size_t(n) * D);
+  distblas::algo::SpMMAlgo<INDEX_TYPE, double, D> algo(g.native.get(), g.receiver.get(), g.sender.get(), &dense,
+                                                       &out, &g.grid, 0.0, 0.25, false, false);
+  reset_performance_timers();
+  algo.algo_spmm(1, batch, lr);
+  std::memcpy(y, out.nCoordinates, sizeof(double) * size_t(n) * D);
+  ::operator delete(dense.nCoordinates);
+  ::operator delete(out.nCoordinates);
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* The reference's SpMM step, SpMMAlgo::algo_spmm(1, batch, lr)
+ * (cpp/algo/spmm.hpp:54-159) as BaselineSpMM::execute runs it
+ * (cpp/algo/baseline_spmm.hpp:63-88): y (n x dim) from x. */
+int deref_spmm(int dim, int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, const double *x,
+               int batch, double lr, double *y) {
+  switch (dim) {
+    case 16: return spmm_dim<16>(n, nnz, rowptr, col, x, batch, lr, y);
+    case 32: return spmm_dim<32>(n, nnz, rowptr, col, x, batch, lr, y);
+    case 64: return spmm_dim<64>(n, nnz, rowptr, col, x, batch, lr, y);
+    case 128: return spmm_dim<128>(n, nnz, rowptr, col, x, batch, lr, y);
+  }
+  return -1;
+}
 
 /* Runs `epochs` epochs of the reference embedding step in place on emb (n x dim,
  * row-major FP64).  lr holds one rate per epoch; use_driver_loop = 1 calls

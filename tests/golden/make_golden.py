@@ -4,7 +4,7 @@ Run here, where the reference sources exist:
     make -C oracle ref && python tests/golden/make_golden.py
 
 Every output comes from oracle/_ref/libderef.so, i.e. the reference's
-EmbeddingAlgo (cpp/algo/algo.hpp), sampler (cpp/core/common.cpp:37-53) and CSR
+EmbeddingAlgo (cpp/algo/algo.hpp), SpMMAlgo (cpp/algo/spmm.hpp), sampler (cpp/core/common.cpp:37-53) and CSR
 builder (cpp/core/csr_local.hpp) compiled unmodified against single-rank
 stand-ins for MPI/MKL/Eigen.  The FP64 restatement in oracle/ is then checked
 against these files bit for bit (tests/test_oracle_golden.py).
@@ -78,7 +78,20 @@ def main():
     c = np.array([1, 2, 0, 1, 0, 3, 3, 2], dtype=np.int64)
     rp, cc = oracle.ref_csr(4, r, c)
     np.savez_compressed(os.path.join(OUT, "csr_small.npz"), coo_row=r, coo_col=c, rowptr=rp, col=cc)
+    write_spmm()
     print("done")
+
+
+def write_spmm():
+    """The reference's SpMM step (SpMMAlgo::algo_spmm, cpp/algo/spmm.hpp:54-159)."""
+    n, rp, col = hand_graph()
+    x = gg.init_embedding(n, 32, 7)
+    np.savez_compressed(os.path.join(OUT, "spmm_hand18_d32.npz"), rowptr=rp, col=col, x=x, batch=5, lr=0.1,
+                        y=oracle.ref_spmm(rp, col, x, 5, 0.1))
+    n, rp, col = gg.rmat_csr(9, 8, seed=5)
+    x = gg.init_embedding(n, 16, 8)
+    np.savez_compressed(os.path.join(OUT, "spmm_rmat9_d16.npz"), rowptr=rp, col=col, x=x, batch=96, lr=0.02,
+                        y=oracle.ref_spmm(rp, col, x, 96, 0.02))
 
 
 if __name__ == "__main__":

@@ -88,3 +88,23 @@ def test_oracle_matches_reference_live():
             pytest.skip("draw hits the reference's undefined path")
         xo, _ = oracle.run(rp, col, x0, 3, 200, 6, lr, quirks=True)
         assert np.array_equal(xr, xo)
+
+
+@pytest.mark.parametrize("name", ["spmm_hand18_d32", "spmm_rmat9_d16"])
+def test_oracle_spmm_bitexact(golden_dir, name):
+    # the reference's SpMM step (SpMMAlgo::algo_spmm, cpp/algo/spmm.hpp:54-159):
+    # the hand graph has edges into its last vertex, which the reference skips
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    y = oracle.spmm(g["rowptr"], g["col"], g["x"], float(g["lr"]), quirks=True)
+    assert np.array_equal(y, g["y"])
+    assert not np.array_equal(oracle.spmm(g["rowptr"], g["col"], g["x"], float(g["lr"]), quirks=False), g["y"]) \
+        or name != "spmm_hand18_d32"
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference harness is only buildable where its sources are")
+def test_oracle_spmm_matches_reference_live():
+    from distembed_gb300 import graphgen as gg
+    n, rp, col = gg.rmat_csr(10, 6, seed=13)
+    x = gg.init_embedding(n, 64, 14)
+    for batch in (64, 300, n):
+        assert np.array_equal(oracle.ref_spmm(rp, col, x, batch, 0.05), oracle.spmm(rp, col, x, 0.05))
