@@ -6,9 +6,12 @@
 // C library's rand(), unseeded), same entry (EmbeddingAlgo::algo_force2_vec_ns
 // through GpuEmbeddingAlgo) and same output file (<output>/embedding.txt,
 // cpp/io/parrallel_IO.hpp:90-146).  Extra flags: -dim (the reference fixes 128
-// at compile time), -precision fp32|bf16, -device.  Flags that select other
-// algorithms of the reference (-spmm, -spgemm, -sparse_embedding, -msbfs) are
-// refused; flags of the multi-rank exchange are accepted and not used.
+// at compile time), -precision fp32|bf16, -device, -csr gpu|host.  -spmm 1 runs
+// the reference's SpMM baseline instead (BaselineSpMM::execute,
+// cpp/algo/baseline_spmm.hpp:52-90: per iteration a fresh DenseMat and one
+// SpMMAlgo::algo_spmm step, timed).  Flags that select the other algorithms of
+// the reference (-spgemm, -sparse_embedding, -msbfs) are refused; flags of the
+// multi-rank exchange are accepted and not used.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -44,6 +47,7 @@ struct Flags {
   double alpha = 0, beta = 0.25, lr = 0.02;
   bool col_major = false, sync_comm = false;
   bool gpu_csr = true;  // -csr gpu|host: where the input's COO -> CSR runs
+  bool spmm = false;    // -spmm 1: the SpMM baseline (cpp/dist_embed.cpp:255-268)
   int precision = DE_PRECISION_FP32;
 };
 
@@ -57,6 +61,43 @@ double run(const Flags &f, SpMat &sp, DenseMat &dense, std::vector<double> &loss
   const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   loss = algo.last_loss();
   return s;
+}
+
+// BaselineSpMM::execute (cpp/algo/baseline_spmm.hpp:52-90) at one rank: per
+// iteration a fresh input DenseMat (U[-1, 1) from rand(), dense_mat.hpp:55-63) and
+// one SpMMAlgo::algo_spmm(1, batch, lr) step into an output DenseMat, timed; the
+// timings are appended to perf_output.
+int run_spmm(const Flags &f, const CSRHandle &csr, int64_t rows, int64_t nnz) {
+  de_options o;
+  de_default_options(&o);
+  o.device = f.device;
+  de_handle *h = nullptr;
+  if (de_create(rows, csr.rowStart.data(), csr.col_idx.data(), nnz, f.dim, &o, &h) != DE_OK) {
+    std::fprintf(stderr, "spmm: %s\n", de_last_error(nullptr));
+    return 1;
+  }
+  std::vector<double> x(size_t(rows) * size_t(f.dim)), y(x.size());
+  std::vector<double> secs;
+  for (int it = 0; it < f.iterations; ++it) {
+    for (double &v : x) v = -1.0 + 2.0 * std::rand() / (RAND_MAX + 1.0);
+    const auto t0 = std::chrono::steady_clock::now();
+    if (de_set_embeddings(h, x.data()) != DE_OK || de_spmm(h, f.batch_size, f.lr, y.data()) != DE_OK) {
+      std::fprintf(stderr, "spmm: %s\n", de_last_error(h));
+      de_destroy(h);
+      return 1;
+    }
+    secs.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    std::printf(" rank 0 SpMM iteration %d completed in %.4f s\n", it, secs.back());
+  }
+  de_destroy(h);
+  if (FILE *pf = std::fopen("perf_output", "a")) {
+    std::fprintf(pf, "{\"algo\":\"SpMM\",\"p\":1,\"data_set\":\"%s\",\"device\":\"GB300\",\"batch\":%d,"
+                     "\"iteration_time_s\":[", f.dataset.c_str(), f.batch_size);
+    for (size_t i = 0; i < secs.size(); ++i) std::fprintf(pf, "%s%.6f", i ? "," : "", secs[i]);
+    std::fprintf(pf, "]}\n");
+    std::fclose(pf);
+  }
+  return 0;
 }
 
 }  // namespace
@@ -80,9 +121,10 @@ int main(int argc, char **argv) {
     else if (!std::strcmp(a, "-device")) f.device = std::atoi(v);
     else if (!std::strcmp(a, "-csr")) f.gpu_csr = std::strcmp(v, "host") != 0;
     else if (!std::strcmp(a, "-precision")) f.precision = std::strcmp(v, "bf16") ? DE_PRECISION_FP32 : DE_PRECISION_BF16;
-    else if ((!std::strcmp(a, "-spmm") || !std::strcmp(a, "-spgemm") || !std::strcmp(a, "-sparse_embedding") ||
-              !std::strcmp(a, "-msbfs")) && std::atoi(v) == 1) {
-      std::fprintf(stderr, "%s: only the force-model embedding is provided by this build\n", a);
+    else if (!std::strcmp(a, "-spmm")) f.spmm = std::atoi(v) == 1;
+    else if ((!std::strcmp(a, "-spgemm") || !std::strcmp(a, "-sparse_embedding") || !std::strcmp(a, "-msbfs")) &&
+             std::atoi(v) == 1) {
+      std::fprintf(stderr, "%s: only the force-model embedding and the SpMM baseline are provided by this build\n", a);
       return 2;
     }
   }
@@ -130,6 +172,7 @@ int main(int argc, char **argv) {
   sp.gCols = cols;
   sp.gNNz = nnz;
   std::printf(" rank 0 gROWs  %lld gCols %lld nnz %lld\n", (long long)rows, (long long)cols, (long long)nnz);
+  if (f.spmm) return run_spmm(f, csr, rows, nnz);
   // ---- initial embedding (cpp/core/dense_mat.hpp:55-63)
   std::vector<double> coords(size_t(rows) * size_t(f.dim));
   for (size_t i = 0; i < coords.size(); ++i) coords[i] = -1.0 + 2.0 * std::rand() / (RAND_MAX + 1.0);

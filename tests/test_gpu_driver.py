@@ -85,3 +85,18 @@ def test_driver_col_major_flag_is_the_one_rank_row_major_pass(tmp_path):
         assert r.returncode == 0, r.stderr
         texts.append((out / "embedding.txt").read_text())
     assert texts[0] == texts[1]
+
+
+def test_driver_spmm_baseline(tmp_path):
+    """-spmm 1: the reference's SpMM baseline (BaselineSpMM::execute,
+    cpp/algo/baseline_spmm.hpp:52-90), one timed SpMM step per iteration."""
+    n, rp, col = gg.knn_csr(700, 8, 6, 3, seed=8)
+    mtx = str(tmp_path / "g.mtx")
+    gg.write_mtx(mtx, n, rp, col)
+    r = subprocess.run([de.DRIVER_PATH, "-input", mtx, "-spmm", "1", "-iter", "3", "-batch", "128", "-dim", "64",
+                        "-lr", "0.02"], capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.count("SpMM iteration") == 3
+    line = [ln for ln in open(tmp_path / "perf_output") if '"SpMM"' in ln][-1]
+    import json
+    assert len(json.loads(line)["iteration_time_s"]) == 3
