@@ -734,7 +734,17 @@ __global__ void __launch_bounds__(256) bf16_apply_kernel(const BF16BatchArgs a) 
   for (int row_local = gw; row_local < a.rows; row_local += gridDim.x * 8) {
     const int row = a.base + row_local;
     uint32_t *bits_row = a.near_bits + size_t(row_local) * kNearWords;
+    // every load of the row at once: the bitmask, the row's CSR extent, the master
+    // row and both updates (the attractive one is used only for rows with CSR
+    // entries: other rows' slots hold an earlier minibatch's values)
     const uint32_t my_word = lane < kNearWords ? bits_row[lane] : 0u;
+    const bool has_attr = __ldg(a.rowptr + row + 1) > __ldg(a.rowptr + row);
+    float *xm = a.xm + size_t(row) * D + lane * N;
+    __nv_bfloat16 *xb = a.xb + size_t(row) * D + lane * N;
+    float mv[N], av[N], rv[N];
+    ld_contig<N>(mv, xm);
+    ld_contig<N>(av, a.abuf + size_t(row_local) * D + lane * N);
+    ld_contig<N>(rv, a.rbuf + size_t(row_local) * D + lane * N);
     Frag<D> acc;
     acc.zero();
     const bool exact = __any_sync(kFull, my_word != 0u);
@@ -769,22 +779,9 @@ __global__ void __launch_bounds__(256) bf16_apply_kernel(const BF16BatchArgs a) 
       if (lane == 0) a.loss_row[row] += double(loss);
     }
     // lane: N consecutive components, moved as 16-byte vectors (8-byte at dim 64)
-    float *xm = a.xm + size_t(row) * D + lane * N;
-    __nv_bfloat16 *xb = a.xb + size_t(row) * D + lane * N;
-    const float *ab = a.abuf + size_t(row_local) * D + lane * N;
-    const float *rb = a.rbuf + size_t(row_local) * D + lane * N;
-    float mv[N], av[N], rv[N];
-    ld_contig<N>(mv, xm);
-    if (__ldg(a.rowptr + row + 1) > __ldg(a.rowptr + row)) {
-      ld_contig<N>(av, ab);
-    } else {  // no CSR entries: the attractive pass wrote nothing for this row
-#pragma unroll
-      for (int t = 0; t < N; ++t) av[t] = 0.f;
-    }
-    ld_contig<N>(rv, rb);
 #pragma unroll
     for (int t = 0; t < N; ++t) {
-      mv[t] = mv[t] + (av[t] + rv[t]);
+      mv[t] = mv[t] + ((has_attr ? av[t] : 0.f) + rv[t]);
       if (exact) mv[t] = mv[t] + acc.v[t];
     }
     st_contig<N>(xm, mv);
