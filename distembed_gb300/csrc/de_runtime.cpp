@@ -688,11 +688,34 @@ int de_destroy(de_handle *h) {
   return DE_OK;
 }
 
+// Device address of host memory the GPU can read and write in place (pinned and
+// mapped, e.g. from cudaHostAlloc), or nullptr.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 static int copy_embeddings_f64(de_handle *h, double *host, bool to_device, float *dev = nullptr) {
   if (!h || !host) return fail(h, DE_ERR_INVALID, "NULL argument");
   DE_CUDA(h, cudaSetDevice(h->device));
   if (!dev) dev = h->d_x;
   const int64_t total = h->n * h->dim;
+  if (double *mapped = static_cast<double *>(mapped_host(host))) {
+    // pinned host memory: the conversion kernel reads or writes it in place, one
+    // pass over the link instead of a copy to a staging buffer and a second pass
+    if (to_device) {
+      DE_CUDA(h, launch_f64_to_f32(mapped, dev, total, h->stream));
+      if (h->d_xb) DE_CUDA(h, launch_f32_to_bf16(dev, h->d_xb, total, h->stream));
+    } else {
+      DE_CUDA(h, launch_f32_to_f64(dev, mapped, total, h->stream));
+    }
+    DE_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DE_OK;
+  }
   const int64_t chunk = std::min<int64_t>(total, int64_t(8) << 20);  // 64 MiB of FP64
   if (int rc = grow(h, &h->d_stage64, &h->stage64_cap, size_t(chunk))) return rc;
   for (int64_t off = 0; off < total; off += chunk) {

@@ -169,6 +169,30 @@ def test_bitwise_reproducible_and_handle_reuse():
         assert np.array_equal(h.get_embeddings(), a)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_pinned_host_buffers_equal_pageable(precision):
+    # pinned host memory is converted in place by the GPU, pageable memory through
+    # a staging copy: the same values either way
+    import torch
+    n, rp, col = gg.rmat_csr(11, 8, seed=25)
+    x0 = f32(gg.init_embedding(n, 128, seed=10))
+    pinned_in = torch.empty((n, 128), dtype=torch.float64, pin_memory=True).numpy()
+    pinned_in[:] = x0
+    pinned_out = torch.empty((n, 128), dtype=torch.float64, pin_memory=True).numpy()
+    out = []
+    for src in (x0, pinned_in):
+        with de.Handle(rp, col, 128, precision=precision) as h:
+            h.set_embeddings(src)
+            loss = h.run(2, 300, 5, 0.02)
+            y = h.get_embeddings(out=pinned_out) if src is pinned_in else h.get_embeddings()
+            out.append((np.array(y), loss))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    with de.Handle(rp, col, 128) as h:
+        h.set_embeddings(pinned_in)
+        assert np.array_equal(h.get_embeddings(), x0)
+        assert np.array_equal(h.spmm(256, 0.1, out=pinned_out), h.spmm(256, 0.1))
+
+
 @pytest.mark.parametrize("dim", [64, 128])
 def test_overlapped_launches_bitwise_equal_to_serial(dim):
     # launch j+1 starts before launch j completes; its early phase must only
