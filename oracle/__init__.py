@@ -55,6 +55,9 @@ def lib():
         L.oracle_run_batches.restype = ctypes.c_int64
         L.oracle_spmm.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_double, ctypes.c_int,
                                   _f64p]
+        L.oracle_sparse_embedding.argtypes = [ctypes.c_int, ctypes.c_int64, _i64p, _i64p, _f64p, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_int, _f64p]
         _LIB = L
     return _LIB
 
@@ -82,6 +85,9 @@ def ref():
         L.deref_csr.argtypes = [ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _i64p, _i64p]
         L.deref_spmm.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p, ctypes.c_int,
                                  ctypes.c_double, _f64p]
+        L.deref_sparse_embedding.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                             ctypes.c_double, ctypes.c_int, _f64p]
         _REF = L
     return _REF
 
@@ -177,6 +183,36 @@ def ref_run(rowptr, col, x, epochs, batch, ns, lr, driver_loop=False):
     if rc != 0:
         raise ValueError(f"deref_run failed ({rc})")
     return x
+
+
+ABSENT = float(-2 ** 31)  # INT_MIN: an absent entry of a sparse embedding row
+
+
+def sparse_embedding(rowptr, col, x, iterations, batch, ns, lr, density, merge=False, quirks=True):
+    """The reference's sparse embedding at one rank (cpp/algo/sparse_embedding.hpp:
+    78-194), FP64: returns (x after the run, batch collector [batch, dim])."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.array(x, dtype=np.float64, order="C")
+    n, dim = x.shape
+    coll = np.zeros((batch, dim), dtype=np.float64)
+    rc = lib().oracle_sparse_embedding(dim, n, _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), iterations, batch,
+                                       ns, lr, density, int(merge), int(quirks), _p(coll, _f64p))
+    if rc != 0:
+        raise ValueError(f"oracle_sparse_embedding failed ({rc})")
+    return x, coll
+
+
+def ref_sparse_embedding(rowptr, col, x, iterations, batch, ns, lr, density, merge=False):
+    """The reference's own SparseEmbedding at one rank (FP64): (x, batch collector)."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.array(x, dtype=np.float64, order="C")
+    n, dim = x.shape
+    coll = np.zeros((batch, dim), dtype=np.float64)
+    rc = ref().deref_sparse_embedding(dim, n, len(col), _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), iterations,
+                                      batch, ns, lr, density, int(merge), _p(coll, _f64p))
+    if rc != 0:
+        raise ValueError(f"deref_sparse_embedding failed ({rc})")
+    return x, coll
 
 
 def ref_spmm(rowptr, col, x, batch, lr):

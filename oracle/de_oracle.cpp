@@ -24,7 +24,9 @@
  *   F9  a negative draw equal to n (the sampler's upper bound is inclusive) makes
  *       the reference index a one-element vector out of range (algo.hpp:605-617).
  *       Such draws contribute nothing here, in both modes.
- * Also: the reference's SpMM step (oracle_spmm, cpp/algo/spmm.hpp:54-159, 358-412).
+ * Also: the reference's SpMM step (oracle_spmm, cpp/algo/spmm.hpp:54-159, 358-412)
+ * and its sparse embedding at one rank (oracle_sparse_embedding,
+ * cpp/algo/sparse_embedding.hpp:78-194, 338-503, 505-659, 745-767).
  * The loss (absent from the reference) is the t-distribution objective whose
  * negative gradient is the force before clipping:
  *   attractive pair  log(1 + r)
@@ -261,6 +263,114 @@ int oracle_spmm(int64_t n, const int64_t *rowptr, const int64_t *col, int dim, c
       for (int d = 0; d < dim; ++d) yi[d] = yi[d] + lr * xc[d];
     }
   }
+  return 0;
+}
+
+/* SparseEmbedding::algo_sparse_embedding at one rank (col_world_size == 1,
+ * cpp/algo/sparse_embedding.hpp:78-194).  Embedding rows are dense FP64 vectors in
+ * which the value INT_MIN marks an absent entry (the dense collector,
+ * cpp/core/sparse_mat.hpp:367-377, 492-505).  Per iteration i and minibatch j
+ * (rows [jB, min(jB + B, n))):
+ *   merge = 0 (the reference's one-rank branch, lines 138-144): the attractive pass
+ *     only.  Its updates go into the batch collector coll [B, dim], slot r for row
+ *     jB + r, which that branch never merges nor clears: coll accumulates over all
+ *     minibatches and iterations and the embedding values do not change.
+ *   merge = 1 (the steps of the multi-rank branch that touch the local partition,
+ *     lines 145-168): the repulsive pass on the minibatch's negatives (seed i + j),
+ *     the attractive pass, then merge_batch_collector (sparse_mat.hpp:385-400):
+ *     x = (x != INT_MIN ? x + coll : coll), coll = 0, for every entry of the rows.
+ * Pair term (both passes, lines 380-427 and 548-598): the union of the two rows'
+ * present entries in ascending dim order; value = x_i - x_j where both are
+ * present, x_i or -x_j where one is; r = sum of value^2 in that order;
+ * attractive d1 = -2 / (1 + r), repulsive d1 = 2 / ((r + 1e-6)(1 + r)); each union
+ * entry k gets coll[k] += lr * clip(value_k * d1), clip at +-5 (lines 737-743).
+ * After every iteration but the last, when floor(present entries / n) > k with
+ * k = (int)(dim * density) (lines 172-181), every row keeps its k largest values
+ * and the other dim - k become INT_MIN (preserveHighestK, lines 745-767; at equal
+ * values the lower index is nullified first, which the reference leaves to its
+ * heap's order).  After the last iteration absent entries become 0 (the final
+ * CSR build with clear_dense_collector, lines 183-186,
+ * cpp/core/distributed_mat.hpp:63-91).  A negative draw equal to n (the reference
+ * would read another rank's cache out of range, lines 516-537) contributes
+ * nothing.  With quirks, F8 holds for the repulsive pass of merge = 1: its row
+ * count (block_size = considering_batch_size, lines 132-137, 146, 510-511) stays
+ * last_batch_size from the last minibatch of the first iteration on.  coll (may
+ * be NULL) receives the batch collector after the run.
+ * Returns 0, or -1 for bad arguments. */
+int oracle_sparse_embedding(int dim, int64_t n, const int64_t *rowptr, const int64_t *col, double *x,
+                            int iterations, int batch, int ns, double lr, double density, int merge, int quirks,
+                            double *coll_out) {
+  if (dim <= 0 || n <= 0 || batch <= 0 || iterations < 0 || ns < 0) return -1;
+  const double kAbsent = double(INT32_MIN);
+  const int k_keep = static_cast<int>(dim * density);
+  const int batches = int(n / batch + (n % batch ? 1 : 0));
+  const int64_t last_batch_size = (n % batch) ? n - int64_t(batch) * (batches - 1) : batch;
+  std::vector<double> coll(size_t(batch) * dim, 0.0);
+  std::vector<int64_t> negs(size_t(std::max(ns, 1)));
+  // one pair of rows: the union walk and the update of coll row `slot`
+  auto pair = [&](int64_t i, int64_t j, bool attract, double *c) {
+    const double *xi = x + i * dim, *xj = x + j * dim;
+    double r = 0.0;
+    for (int d = 0; d < dim; ++d) {
+      const bool pi = xi[d] != kAbsent, pj = xj[d] != kAbsent;
+      if (!pi && !pj) continue;
+      const double v = (pi && pj) ? xi[d] - xj[d] : (pi ? xi[d] : -1 * xj[d]);
+      r += v * v;
+    }
+    const double d1 = attract ? -2.0 / (1.0 + r) : 2.0 / ((r + 0.000001) * (1.0 + r));
+    for (int d = 0; d < dim; ++d) {
+      const bool pi = xi[d] != kAbsent, pj = xj[d] != kAbsent;
+      if (!pi && !pj) continue;
+      const double v = (pi && pj) ? xi[d] - xj[d] : (pi ? xi[d] : -1 * xj[d]);
+      c[d] += lr * clip(v * d1);
+    }
+  };
+  for (int it = 0; it < iterations; ++it) {
+    for (int j = 0; j < batches; ++j) {
+      const int64_t base = int64_t(j) * batch;
+      const int64_t rows = (j == batches - 1) ? last_batch_size : batch;
+      if (merge) {
+        negatives(n, j + it, ns, negs.data());
+        const int64_t rep_rows = (quirks && it > 0) ? last_batch_size : rows;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t r = 0; r < rep_rows; ++r)
+          for (int q = 0; q < ns; ++q)
+            if (negs[q] >= 0 && negs[q] < n) pair(base + r, negs[q], false, coll.data() + r * dim);
+      }
+#pragma omp parallel for schedule(dynamic, 64)
+      for (int64_t r = 0; r < rows; ++r)
+        for (int64_t e = rowptr[base + r]; e < rowptr[base + r + 1]; ++e)
+          pair(base + r, col[e], true, coll.data() + r * dim);
+      if (merge) {
+        for (int64_t r = 0; r < rows; ++r)
+          for (int d = 0; d < dim; ++d) {
+            double &xv = x[(base + r) * dim + d];
+            double &cv = coll[size_t(r) * dim + d];
+            xv = (xv != kAbsent) ? xv + cv : cv;
+            cv = 0.0;
+          }
+      }
+    }
+    if (it < iterations - 1) {
+      int64_t present = 0;
+      for (int64_t e = 0; e < n * dim; ++e) present += x[e] != kAbsent;
+      const int per_row = static_cast<int>(double(present) / double(n));
+      if (per_row > k_keep) {
+        const int nullify = dim - k_keep;
+        std::vector<int> idx(dim);
+        for (int64_t i = 0; i < n; ++i) {
+          double *xi = x + i * dim;
+          for (int d = 0; d < dim; ++d) idx[d] = d;
+          std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return xi[a] < xi[b]; });
+          for (int q = 0; q < nullify && q < dim; ++q) xi[idx[q]] = kAbsent;
+        }
+      }
+    } else {
+      for (int64_t e = 0; e < n * dim; ++e)
+        if (x[e] == kAbsent) x[e] = 0.0;
+    }
+  }
+  if (coll_out) std::memcpy(coll_out, coll.data(), coll.size() * sizeof(double));
   return 0;
 }
 

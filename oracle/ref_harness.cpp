@@ -1,9 +1,9 @@
 /*
  * TEST INFRASTRUCTURE ONLY — never linked into the product.
  *
- * Drives the reference's own embedding step and SpMM step, compiled unmodified
- * from their sources (cpp/algo/algo.hpp, cpp/algo/spmm.hpp, cpp/core/common.cpp,
- * cpp/net/process_3D_grid.cpp)
+ * Drives the reference's own embedding step, SpMM step and sparse embedding,
+ * compiled unmodified from their sources (cpp/algo/algo.hpp, cpp/algo/spmm.hpp,
+ * cpp/algo/sparse_embedding.hpp, cpp/core/common.cpp, cpp/net/process_3D_grid.cpp)
  * against the single-rank stand-ins in oracle/shim/.  It exposes a small C ABI
  * used to (1) pin the FP64 restatement in oracle/de_oracle.cpp bit-for-bit and
  * (2) write the golden vectors under tests/golden/.
@@ -16,6 +16,7 @@
  * alpha 0, beta 0.25, bounds +-5, row-major, async comm (the driver defaults).
  */
 #include "algo/algo.hpp"
+#include "algo/sparse_embedding.hpp"
 #include "algo/spmm.hpp"
 
 #include <cstring>
@@ -148,9 +149,75 @@ int spmm_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, 
   return 0;
 }
 
+template <size_t D>
+int sparse_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, double *x, int iterations,
+               int batch, int ns, double lr, double density, int merge, double *coll) {
+  const int batches = int(n / batch + (n % batch ? 1 : 0));
+  // merge = 1 runs the repulsive pass, whose draw equal to gRows reads another
+  // rank's cache out of range (cpp/algo/sparse_embedding.hpp:516-537)
+  if (merge && !draws_in_range(n, iterations, batches, ns)) return -2;
+  RefGraph g(n, nnz, rowptr, col, batch);
+  // the output matrix as the driver makes it (cpp/dist_embed.cpp:318), holding
+  // the caller's values instead of rand() ones
+  SpMat<double> out(&g.grid, INDEX_TYPE(n), INDEX_TYPE(D), false, false);
+  for (int64_t i = 0; i < n; ++i)
+    for (size_t d = 0; d < D; ++d) (*out.dense_collector)[i][d] = x[i * int64_t(D) + int64_t(d)];
+  distblas::algo::SparseEmbedding<INDEX_TYPE, double, D> se(g.native.get(), g.receiver.get(), g.sender.get(), &out,
+                                                           &g.grid, 0.0, 0.25, false, true, 0.5, false);
+  // algo_sparse_embedding's one-rank loop (cpp/algo/sparse_embedding.hpp:78-194)
+  // without the tile communicator, which the one-rank branch does not use; with
+  // merge = 1 the local steps of the multi-rank branch (lines 145-168)
+  const int expected_nnz_per_row = static_cast<int>(D * density);
+  out.initialize_CSR_blocks(false, nullptr, static_cast<double>(INT_MIN), false);
+  const int last_batch_size = (n % batch) ? int(n - int64_t(batch) * (batches - 1)) : batch;
+  out.initialize_batch_collector(batch);
+  CSRLocal<double> *csr_block = g.native->csr_local_data.get();
+  int considering_batch_size = batch;
+  for (int i = 0; i < iterations; ++i) {
+    for (int j = 0; j < batches; ++j) {
+      if (j == batches - 1) considering_batch_size = last_batch_size;
+      vector<INDEX_TYPE> negs = generate_random_numbers(0, int(g.gRows), j + i, ns);
+      if (merge) se.calc_t_dist_replus_rowptr(negs, lr, j, batch, considering_batch_size, &out);
+      se.calc_t_dist_grad_rowptr(csr_block, lr, i, j, batch, considering_batch_size, 0, 0, 0, false, nullptr, &out);
+      if (merge) out.merge_batch_collector(j, batch);
+    }
+    if (i < iterations - 1) {
+      out.initialize_CSR_blocks(false, nullptr, static_cast<double>(INT_MIN), false);
+      size_t size_r = out.csr_local_data->handler->rowStart.size();
+      double output_nnz = out.csr_local_data->handler->rowStart[size_r - 1];
+      auto output_nnz_per_row = static_cast<int>(output_nnz / g.receiver->proc_row_width);
+      if (output_nnz_per_row > expected_nnz_per_row)
+        se.preserveHighestK(out.dense_collector.get(), expected_nnz_per_row, static_cast<double>(INT_MIN));
+    } else {
+      out.initialize_CSR_blocks(false, nullptr, static_cast<double>(INT_MIN), true);
+    }
+  }
+  for (int64_t i = 0; i < n; ++i)
+    for (size_t d = 0; d < D; ++d) x[i * int64_t(D) + int64_t(d)] = (*out.dense_collector)[i][d];
+  if (coll)
+    for (int r = 0; r < batch; ++r)
+      for (size_t d = 0; d < D; ++d) coll[size_t(r) * D + d] = (*out.batch_collector)[r][d];
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* The reference's sparse embedding at one rank (cpp/algo/sparse_embedding.hpp:
+ * 78-194): x (n x dim, INT_MIN = absent) in place; coll (batch x dim, may be
+ * NULL) receives the batch collector.  Returns 0, -1 for an unsupported dim, -2
+ * when merge = 1 and a negative draw would hit the out-of-range path. */
+int deref_sparse_embedding(int dim, int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, double *x,
+                           int iterations, int batch, int ns, double lr, double density, int merge, double *coll) {
+  switch (dim) {
+    case 16: return sparse_dim<16>(n, nnz, rowptr, col, x, iterations, batch, ns, lr, density, merge, coll);
+    case 32: return sparse_dim<32>(n, nnz, rowptr, col, x, iterations, batch, ns, lr, density, merge, coll);
+    case 64: return sparse_dim<64>(n, nnz, rowptr, col, x, iterations, batch, ns, lr, density, merge, coll);
+    case 128: return sparse_dim<128>(n, nnz, rowptr, col, x, iterations, batch, ns, lr, density, merge, coll);
+  }
+  return -1;
+}
 
 /* The reference's SpMM step, SpMMAlgo::algo_spmm(1, batch, lr)
  * (cpp/algo/spmm.hpp:54-159) as BaselineSpMM::execute runs it

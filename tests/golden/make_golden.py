@@ -79,6 +79,7 @@ def main():
     rp, cc = oracle.ref_csr(4, r, c)
     np.savez_compressed(os.path.join(OUT, "csr_small.npz"), coo_row=r, coo_col=c, rowptr=rp, col=cc)
     write_spmm()
+    write_sparse()
     print("done")
 
 
@@ -92,6 +93,22 @@ def write_spmm():
     x = gg.init_embedding(n, 16, 8)
     np.savez_compressed(os.path.join(OUT, "spmm_rmat9_d16.npz"), rowptr=rp, col=col, x=x, batch=96, lr=0.02,
                         y=oracle.ref_spmm(rp, col, x, 96, 0.02))
+
+
+
+def write_sparse():
+    """The reference's sparse embedding at one rank (SparseEmbedding::algo_sparse_embedding,
+    cpp/algo/sparse_embedding.hpp:78-194): the one-rank branch (merge 0) and the
+    local steps of the multi-rank branch (merge 1)."""
+    cases = [("sparse_hand18_d16_q", hand_graph(), 16, dict(iterations=3, batch=5, ns=3, lr=0.1, density=0.5,
+                                                                merge=0)),
+             ("sparse_rmat9_d16_m", gg.rmat_csr(9, 8, seed=6), 16, dict(iterations=4, batch=100, ns=5, lr=0.1,
+                                                                          density=0.5, merge=1))]
+    for name, (n, rp, col), dim, kw in cases:
+        x = gg.init_embedding(n, dim, 9)
+        xo, coll = oracle.ref_sparse_embedding(rp, col, x, kw["iterations"], kw["batch"], kw["ns"], kw["lr"],
+                                               kw["density"], bool(kw["merge"]))
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), rowptr=rp, col=col, x=x, x_out=xo, coll=coll, **kw)
 
 
 if __name__ == "__main__":

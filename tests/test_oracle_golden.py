@@ -108,3 +108,40 @@ def test_oracle_spmm_matches_reference_live():
     x = gg.init_embedding(n, 64, 14)
     for batch in (64, 300, n):
         assert np.array_equal(oracle.ref_spmm(rp, col, x, batch, 0.05), oracle.spmm(rp, col, x, 0.05))
+
+
+@pytest.mark.parametrize("name", ["sparse_hand18_d16_q", "sparse_rmat9_d16_m"])
+def test_oracle_sparse_embedding_bitexact(golden_dir, name):
+    # the reference's sparse embedding at one rank (cpp/algo/sparse_embedding.hpp:78-194):
+    # embedding values and batch collector equal to the reference's, bit for bit
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    x, coll = oracle.sparse_embedding(g["rowptr"], g["col"], g["x"], int(g["iterations"]), int(g["batch"]),
+                                      int(g["ns"]), float(g["lr"]), float(g["density"]), bool(g["merge"]))
+    assert np.array_equal(x, g["x_out"]) and np.array_equal(coll, g["coll"])
+    if bool(g["merge"]):
+        # the repulsive row count of the multi-rank branch (F8) matters here
+        x2, _ = oracle.sparse_embedding(g["rowptr"], g["col"], g["x"], int(g["iterations"]), int(g["batch"]),
+                                        int(g["ns"]), float(g["lr"]), float(g["density"]), True, quirks=False)
+        assert not np.array_equal(x2, g["x_out"])
+    else:
+        # the one-rank branch never merges its collector: the values are the
+        # input's with the dim - k smallest of every row set to zero
+        k = int(g["x"].shape[1] * float(g["density"]))
+        kept = (g["x_out"] != 0).sum(1)
+        assert np.all(kept == k) and np.all(np.isin(g["x_out"][g["x_out"] != 0], g["x"]))
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference harness is only buildable where its sources are")
+@pytest.mark.parametrize("merge", [False, True])
+def test_oracle_sparse_embedding_matches_reference_live(merge):
+    from distembed_gb300 import graphgen as gg
+    cases = [(gg.rmat_csr(10, 8, seed=21), 32, 3, 97, 0.3), (gg.knn_csr(1200, 8, 8, 4, seed=22), 64, 3, 256, 0.5),
+             (gg.rmat_csr(9, 4, seed=23), 16, 2, 512, 1.0), (gg.rmat_csr(9, 4, seed=24), 16, 3, 50, 0.0)]
+    for (n, rp, col), dim, iters, batch, density in cases:
+        x = gg.init_embedding(n, dim, 25)
+        try:
+            want = oracle.ref_sparse_embedding(rp, col, x, iters, batch, 5, 0.05, density, merge)
+        except ValueError:  # a draw equal to n: the reference's out-of-range path
+            continue
+        got = oracle.sparse_embedding(rp, col, x, iters, batch, 5, 0.05, density, merge)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
