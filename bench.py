@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="max CSR entries per work item (0: automatic)")
-    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched", "served", "spmm"],
+    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched", "served", "spmm", "sparse"],
                    help="plain: FP32 plain form on R-MAT s20 (default line); bf16: BF16 precision form vs the "
                         "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives; batched: 512 graphs in one "
                         "persistent launch, BF16 storage, vs the FP32 plain form on the same graphs")
@@ -874,6 +874,112 @@ def run_spmm_form(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sparse_form(args):
+    """The sparse embedding (SparseEmbedding::algo_sparse_embedding at one rank, the
+    reference's one-rank branch) on the plain workload's graph: one step = one run of
+    5 iterations at density 0.5 from the same FP64 rows, copied in on the device."""
+    import torch
+
+    import distembed_gb300 as de
+    import oracle
+    torch.cuda.set_device(0)
+    n, rowptr, col, x0 = workload()
+    dim, B, lr, ns = W["dim"], W["batch"], W["lr"], W["ns"]
+    iters, density = 5, 0.5
+    keep = int(dim * density)
+    x0 = x0.astype(np.float32).astype(np.float64)
+    nnz = int(len(col))
+    h = de.Handle(rowptr, col, dim, quirks=True)
+    stream = torch.cuda.ExternalStream(h.stream, device=0)
+    x_dev = torch.from_numpy(x0).to("cuda")
+    torch.cuda.synchronize()
+
+    def step():
+        h.sparse_set(x_dev)
+        h.sparse_run(iters, B, ns, lr, density)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev[0].record(stream)
+    for k in range(args.steps):
+        step()
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    step_s = statistics.mean(ms) / 1e3
+    value = nnz * iters / step_s
+    # Algorithmic bytes of a step.  Per iteration the attractive pass reads every
+    # CSR entry's column id and FP32 neighbour row, each row's own row and work
+    # item, and writes its FP32 update; the collector pass reads the updates and
+    # reads and writes the FP64 collector.  Once per step: the FP64 rows copied in
+    # (read + write) and mirrored (read FP64, write FP32); after every iteration but
+    # the last the present entries are counted (read FP64); the pruning after the
+    # first iteration reads FP64 and writes the dim - k dropped entries in FP64 and
+    # FP32; the final pass reads FP64 and writes the absent entries.
+    row32, row64 = 4 * dim, 8 * dim
+    per_iter = nnz * (4 + row32) + n * (row32 + 32 + row32) + n * row32 + 2 * B * row64
+    once = 2 * n * row64 + n * (row64 + row32) + (iters - 1) * n * row64 + n * row64 + n * (dim - keep) * 12 \
+        + n * row64 + n * (dim - keep) * 8
+    alg = iters * per_iter + once
+    peak, peak_kind = measured_peak()
+    # end to end: host FP64 rows in, the run, host FP64 rows and collector out
+    e2e = None
+    if args.e2e_steps > 0:
+        x_host = torch.empty((n, dim), dtype=torch.float64, pin_memory=True).numpy()
+        ts = []
+        for k in range(args.e2e_steps + 1):
+            x_host[:] = x0
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            out_x, out_c = h.sparse_embedding(x_host, iters, B, ns, lr, density)
+            if k > 0:
+                ts.append(time.perf_counter() - t1)
+        e2e = {"value": nnz * iters / statistics.mean(ts), "unit": UNIT, "h2d_bytes_per_step": n * row64,
+               "d2h_bytes_per_step": n * row64 + B * row64, "ms_per_step": 1e3 * statistics.mean(ts),
+               "step": "host FP64 rows in, 5 iterations, host FP64 rows and batch collector out"}
+    # parity and the CPU baseline: 2 iterations (one pruning) on the GPU and in the
+    # FP64 oracle (OpenMP over the host cores)
+    parity, cpu = None, None
+    if not args.no_cpu_baseline:
+        gx, gc = h.sparse_embedding(x0, 2, B, ns, lr, density)
+        t1 = time.perf_counter()
+        ox, oc = oracle.sparse_embedding(rowptr, col, x0, 2, B, ns, lr, density)
+        cs = time.perf_counter() - t1
+        cpu = {"value": nnz * 2 / cs, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"2 iterations of the same run, FP64, {nnz} CSR entries each, in {cs:.2f} s"}
+        parity = {"rows_bitwise_equal_fp64_oracle": bool(np.array_equal(gx, ox)),
+                  "collector_rel_l2_vs_fp64_oracle": float(np.linalg.norm(gc - oc) / np.linalg.norm(oc))}
+    h.close()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 arithmetic on f64 rows",
+            "data": "synthetic: R-MAT scale 20 (ef 16, a.57 b.19 c.19, seed 1), U[-0.5,0.5] init (seed 0)",
+            "config": {"workload": "rmat20_ef16_d128_b4096_sparse_embedding", "n": n, "nnz": nnz, "dim": dim,
+                       "batch": B, "lr": lr, "iterations_per_step": iters, "density": density,
+                       "step": "SparseEmbedding::algo_sparse_embedding, one-rank branch: rows copied in on the "
+                               "device, 5 iterations (attractive pass into the batch collector, top-k pruning "
+                               "after the first), absent entries cleared",
+                       "unit_note": "edge-updates here: attractive pair terms (CSR entries x iterations)",
+                       "l2": "inputs larger than L2 (1 GiB FP64 rows, 512 MiB mirror); no flush"},
+            "roofline": {"bound": "hbm", "kernel": "sparse step (sparse_attract_kernel<128> 5x, collect 5x, "
+                                                  "count + prune, mirror, finalize)",
+                         "achieved": alg / step_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / step_s / 1e9 / peak, "peak_source": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_step": alg,
+                         "note": "algorithmic bytes count every neighbour row gathered, no reuse credited; hub "
+                                 "rows hit in L2, so DRAM moves fewer bytes than counted"},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": args.steps * (1 + 2 * iters + 2 * (iters - 1) + 1),
+            "parity": parity}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -886,6 +992,8 @@ def main():
         run_served_form(args)
     elif args.form == "spmm":
         run_spmm_form(args)
+    elif args.form == "sparse":
+        run_sparse_form(args)
     else:
         run_ours(args)
 

@@ -39,7 +39,8 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
            "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error",
            "de_mm_read", "de_embedding_write", "de_mm_read_gpu", "de_coo_to_csr", "de_csr_info", "de_csr_copy",
-           "de_csr_free", "de_spmm", "de_spmm_f32")
+           "de_csr_free", "de_spmm", "de_spmm_f32", "de_sparse_embedding", "de_sparse_set", "de_sparse_run",
+           "de_sparse_get")
 
 
 class BatchShape(ctypes.Structure):
@@ -165,6 +166,10 @@ def lib():
         L.de_mm_read_gpu.argtypes = [ctypes.c_char_p, _i32, _vp]
         L.de_spmm.argtypes = [_vp, _i32, ctypes.c_double, _vp]
         L.de_spmm_f32.argtypes = [_vp, _i32, ctypes.c_float, _vp, _i32]
+        L.de_sparse_embedding.argtypes = [_vp, _vp, _i32, _i32, _i32, ctypes.c_double, ctypes.c_double, _i32, _vp]
+        L.de_sparse_set.argtypes = [_vp, _vp]
+        L.de_sparse_run.argtypes = [_vp, _i32, _i32, _i32, ctypes.c_double, ctypes.c_double, _i32]
+        L.de_sparse_get.argtypes = [_vp, _vp, _vp]
         L.de_coo_to_csr.argtypes = [_i64, _i64, _vp, _vp, _i64, _i32, _i32, _vp]
         L.de_csr_info.argtypes = [_vp, _vp, _vp, _vp]
         L.de_csr_copy.argtypes = [_vp, _vp, _vp]
@@ -347,6 +352,51 @@ class Handle:
         else:
             self._check(lib().de_spmm(self._h, batch_size, lr, out.ctypes.data))
         return out
+
+    # INT_MIN: an absent entry of a sparse embedding row (the reference's marker)
+    ABSENT = float(-2 ** 31)
+
+    def sparse_embedding(self, x, iterations: int, batch_size: int, ns: int, lr: float, density: float,
+                         merge: bool = False):
+        """The reference's sparse embedding at one rank (SparseEmbedding::algo_sparse_embedding,
+        cpp/algo/sparse_embedding.hpp:78-194) on the handle's graph.  x: FP64 n x dim rows,
+        Handle.ABSENT marking an absent entry.  Returns (rows after the run with absent
+        entries as 0, batch collector [batch_size, dim]).  merge=False is the reference's
+        one-rank branch (the collector is never merged; the rows change only by the top-k
+        pruning); merge=True merges the collector into the rows after every minibatch,
+        with the repulsive pass first, as the multi-rank branch does."""
+        out = np.array(x, dtype=np.float64, order="C")
+        if out.shape != (self.n, self.dim):
+            raise ValueError(f"x must be {self.n} x {self.dim}")
+        coll = np.zeros((batch_size, self.dim), dtype=np.float64)
+        self._check(lib().de_sparse_embedding(self._h, out.ctypes.data, iterations, batch_size, ns, lr, density,
+                                              int(merge), coll.ctypes.data))
+        return out, coll
+
+    def sparse_set(self, x):
+        """Copy sparse embedding rows (FP64 n x dim, Handle.ABSENT = absent) in: a host
+        array, or a contiguous CUDA FP64 tensor (a device-to-device copy)."""
+        if hasattr(x, "is_cuda") and x.is_cuda:
+            if tuple(x.shape) != (self.n, self.dim) or str(x.dtype) != "torch.float64" or not x.is_contiguous():
+                raise ValueError(f"x must be a contiguous FP64 {self.n} x {self.dim} tensor")
+            self._check(lib().de_sparse_set(self._h, x.data_ptr()))
+            return
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (self.n, self.dim):
+            raise ValueError(f"x must be {self.n} x {self.dim}")
+        self._check(lib().de_sparse_set(self._h, x.ctypes.data))
+
+    def sparse_run(self, iterations: int, batch_size: int, ns: int, lr: float, density: float,
+                   merge: bool = False):
+        """Enqueue a sparse embedding run on the device-resident rows (returns at once)."""
+        self._check(lib().de_sparse_run(self._h, iterations, batch_size, ns, lr, density, int(merge)))
+
+    def sparse_get(self, batch_size: int = 0):
+        """Wait for the run and return (rows, batch collector or None)."""
+        x = np.empty((self.n, self.dim), dtype=np.float64)
+        coll = np.empty((batch_size, self.dim), dtype=np.float64) if batch_size > 0 else None
+        self._check(lib().de_sparse_get(self._h, x.ctypes.data, coll.ctypes.data if coll is not None else None))
+        return x, coll
 
     def close(self):
         if getattr(self, "_h", None):

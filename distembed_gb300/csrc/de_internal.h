@@ -66,6 +66,7 @@ struct PlainBatchArgs {
   int32_t batch_id, batches, last_batch_size;
   int32_t n;
   int32_t quirks, compute_loss;
+  int32_t skip_last;        // F7: edges into vertex n-1 are dropped
   float bound;
   const int32_t *negs;      // [epochs, batches, ns]
   int32_t ns;
@@ -106,6 +107,7 @@ struct SpmmArgs {
   float lr;
   float *P;
   int32_t *counters;
+  float bound;  // sparse embedding: clip bound of the attractive force
 };
 
 // Kernel arguments of one minibatch of the BF16 precision form.
@@ -185,6 +187,18 @@ int copy_loss(de_handle *h, double *out, int32_t epochs);
 cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool pdl, cudaStream_t s);
 cudaError_t launch_flush(int dim, const FlushArgs &a, bool pdl, cudaStream_t s);
 cudaError_t launch_spmm(int dim, const SpmmArgs &a, cudaStream_t s);
+
+// Sparse embedding (de_sparse.cu).  Rows are FP64 vectors with INT_MIN marking
+// an absent entry; their FP32 mirror holds 0 there.
+cudaError_t launch_sparse_attract(int dim, const SpmmArgs &a, cudaStream_t s);
+cudaError_t launch_sparse_collect(const float *y, double *coll, int64_t n, int32_t batch, int32_t dim,
+                                  cudaStream_t s);
+cudaError_t launch_sparse_mirror(const double *x64, float *x32, int64_t count, cudaStream_t s);
+cudaError_t launch_sparse_count(const double *x64, int64_t count, unsigned long long *present, cudaStream_t s);
+cudaError_t launch_sparse_prune_f64(int dim, double *x64, float *x32, int64_t n, int32_t keep,
+                                    const unsigned long long *present, cudaStream_t s);
+cudaError_t launch_sparse_prune_f32(int dim, float *x32, int64_t n, int32_t keep, cudaStream_t s);
+cudaError_t launch_sparse_finalize(double *x64, int64_t count, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *src, float *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int64_t count, cudaStream_t s);
 constexpr int kPlainWarps = 4;      // warps per CTA of the plain batch kernel

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
   const int epoch = a.epoch[0];
   const float lr = a.lr[epoch];
   const float bound = a.bound;
-  const int skip = a.quirks ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
+  const int skip = a.skip_last ? a.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
   // this item's CSR entries, one per lane (at most 32)
   const int cnt = has_item ? it.e_end - it.e_begin : 0;
   int ids = -1;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,6 +55,15 @@ struct de_handle {
   float *d_y = nullptr;      // SpMM output [n, dim]
   int32_t *d_spmm_off = nullptr;  // SpMM: per-minibatch first partial slot, then first counter
   int spmm_batch = 0, spmm_cap = 0;
+  // sparse embedding: FP64 rows (INT_MIN = absent; d_x holds their FP32 mirror),
+  // the batch collector [B, dim] and the present-entry count
+  double *d_sx = nullptr;
+  double *d_coll = nullptr;
+  size_t coll_cap = 0;
+  unsigned long long *d_present = nullptr;
+  int sparse_batch = 0;
+  bool sparse_in_mirror = false;  // the last run's result is in d_x (merge = 1)
+  bool keep_last_edges = false;   // F7 off for the plain pass (the sparse embedding's merge = 1)
   int64_t spmm_parts = 0, spmm_split = 0;
   size_t stage_cap = 0;
   float *d_parts = nullptr;
@@ -430,6 +440,7 @@ cudaError_t enqueue_epoch_plain(de_handle *h, int ns, cudaStream_t st, cudaEvent
     a.last_batch_size = s.last_batch_size;
     a.n = int32_t(h->n);
     a.quirks = h->opt.ref_quirks;
+    a.skip_last = h->opt.ref_quirks && !h->keep_last_edges;
     a.compute_loss = h->opt.compute_loss;
     a.bound = float(h->opt.max_bound);
     a.negs = h->d_negs;
@@ -651,6 +662,9 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->sched.d_items);
   dev_free(h, h->d_stage);
   dev_free(h, h->d_y);
+  dev_free(h, h->d_sx);
+  dev_free(h, h->d_coll);
+  dev_free(h, h->d_present);
   dev_free(h, h->d_spmm_off);
   dev_free(h, h->d_parts);
   dev_free(h, h->d_counters);
@@ -839,9 +853,9 @@ int de_run_from(de_handle *h, int32_t first_epoch, int32_t epochs, int32_t batch
   return DE_OK;
 }
 
-// SpMMAlgo::algo_spmm(1, batch_size, lr) at one rank (cpp/algo/spmm.hpp:54-159):
-// the rows of each minibatch into d_y from the current embedding.
-static int spmm_run(de_handle *h, int32_t batch_size, double lr) {
+// Work list, partial slots, counters and output rows of a one-launch pass over
+// every minibatch (the SpMM step and the sparse embedding's attractive pass).
+static int spmm_layout(de_handle *h, int32_t batch_size) {
   if (batch_size <= 0) return fail(h, DE_ERR_INVALID, "batch_size > 0");
   DE_CUDA(h, cudaSetDevice(h->device));
   if (int rc = ensure_schedule(h, batch_size)) return rc;
@@ -873,6 +887,14 @@ static int spmm_run(de_handle *h, int32_t batch_size, double lr) {
   if (counters_moved) DE_CUDA(h, cudaMemsetAsync(h->d_counters, 0, h->counters_cap * sizeof(int32_t), h->stream));
   if (moved || counters_moved) drop_graph(h);
   if (!h->d_y) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_y), size_t(h->n) * h->dim * sizeof(float)));
+  return DE_OK;
+}
+
+// SpMMAlgo::algo_spmm(1, batch_size, lr) at one rank (cpp/algo/spmm.hpp:54-159):
+// the rows of each minibatch into d_y from the current embedding.
+static int spmm_run(de_handle *h, int32_t batch_size, double lr) {
+  if (int rc = spmm_layout(h, batch_size)) return rc;
+  const Schedule &s = h->sched;
   SpmmArgs a{};
   a.X = h->d_x;
   a.Y = h->d_y;
@@ -903,6 +925,129 @@ int de_spmm_f32(de_handle *h, int32_t batch_size, float lr, float *y, int32_t on
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
   DE_CUDA(h, cudaStreamSynchronize(h->stream));
   return DE_OK;
+}
+
+// ---------------------------------------------------------------- sparse embedding
+// SparseEmbedding::algo_sparse_embedding at one rank (cpp/algo/sparse_embedding.hpp:
+// 78-194).  merge = 0: the one-rank branch, whose attractive updates go into the
+// batch collector and are never merged (the values change only by the top-k
+// pruning after the first iteration); merge = 1: per minibatch the repulsive
+// pass, the attractive pass and the merge of the collector into the rows (the
+// steps of the multi-rank branch that touch the local partition), which is the
+// FP32 plain minibatch step on the mirror with edges into n - 1 kept.
+
+int de_sparse_set(de_handle *h, const double *x) {
+  if (!h || !x) return DE_ERR_INVALID;
+  if (h->opt.precision != DE_PRECISION_FP32)
+    return fail(h, DE_ERR_UNSUPPORTED, "the sparse embedding runs on an FP32 handle");
+  if (h->dim != 32 && h->dim != 64 && h->dim != 128 && h->dim != 256)
+    return fail(h, DE_ERR_UNSUPPORTED, "the sparse embedding supports dim 32, 64, 128 or 256");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  const size_t count = size_t(h->n) * h->dim;
+  if (!h->d_sx) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_sx), count * sizeof(double)));
+  if (!h->d_present) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_present), sizeof(unsigned long long)));
+  // x is host or device memory (unified addressing tells which)
+  DE_CUDA(h, cudaMemcpyAsync(h->d_sx, x, count * sizeof(double), cudaMemcpyDefault, h->stream));
+  DE_CUDA(h, launch_sparse_mirror(h->d_sx, h->d_x, int64_t(count), h->stream));
+  h->sparse_in_mirror = false;
+  return DE_OK;
+}
+
+int de_sparse_run(de_handle *h, int32_t iterations, int32_t batch_size, int32_t ns, double lr, double density,
+                  int32_t merge) {
+  if (!h) return DE_ERR_INVALID;
+  if (!h->d_sx) return fail(h, DE_ERR_INVALID, "no sparse embedding rows: call de_sparse_set first");
+  if (iterations < 0 || batch_size <= 0 || ns < 0 || !std::isfinite(density))
+    return fail(h, DE_ERR_INVALID, "iterations >= 0, batch_size > 0, ns >= 0, finite density");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  // expected_nnz_per_row = static_cast<int>(embedding_dim * density) (line 86)
+  const double kd = double(h->dim) * density;
+  const int32_t keep = int32_t(std::max(-1.0, std::min(kd, double(h->dim) + 1.0)));
+  const int64_t count = h->n * int64_t(h->dim);
+  int rc = DE_OK;
+  // the batch collector starts at zero (initialize_batch_collector, line 95)
+  bool moved = false;
+  if ((rc = grow(h, &h->d_coll, &h->coll_cap, size_t(batch_size) * h->dim, &moved))) return rc;
+  DE_CUDA(h, cudaMemsetAsync(h->d_coll, 0, size_t(batch_size) * h->dim * sizeof(double), h->stream));
+  h->sparse_batch = batch_size;
+  h->sparse_in_mirror = false;
+  if (iterations == 0) return DE_OK;
+  if (!merge) {
+    if ((rc = spmm_layout(h, batch_size))) return rc;
+    const Schedule &s = h->sched;
+    SpmmArgs a{};
+    a.X = h->d_x;
+    a.Y = h->d_y;
+    a.col = h->d_col;
+    a.items = s.d_items;
+    a.n_items = s.n_items;
+    a.batch = s.batch;
+    a.slot_off = h->d_spmm_off;
+    a.counter_off = h->d_spmm_off + s.batches + 1;
+    a.skip = -1;
+    a.lr = float(lr);
+    a.P = h->d_parts;
+    a.counters = h->d_counters;
+    a.bound = float(h->opt.max_bound);
+    for (int it = 0; it < iterations; ++it) {
+      DE_CUDA(h, launch_sparse_attract(h->dim, a, h->stream));
+      DE_CUDA(h, launch_sparse_collect(h->d_y, h->d_coll, h->n, batch_size, h->dim, h->stream));
+      if (it < iterations - 1) {
+        DE_CUDA(h, cudaMemsetAsync(h->d_present, 0, sizeof(unsigned long long), h->stream));
+        DE_CUDA(h, launch_sparse_count(h->d_sx, count, h->d_present, h->stream));
+        DE_CUDA(h, launch_sparse_prune_f64(h->dim, h->d_sx, h->d_x, h->n, keep, h->d_present, h->stream));
+      } else {
+        DE_CUDA(h, launch_sparse_finalize(h->d_sx, count, h->stream));
+      }
+    }
+    return DE_OK;
+  }
+  // merge = 1: every entry of a row is present after its minibatch's merge
+  // (merge_batch_collector writes all of them, cpp/core/sparse_mat.hpp:385-400),
+  // so at the end of an iteration floor(present / n) = dim and the rows are
+  // pruned whenever keep < dim; the pruned entries read as 0 in the mirror.
+  h->keep_last_edges = true;
+  drop_graph(h);
+  for (int it = 0; it < iterations && rc == DE_OK; ++it) {
+    rc = de_run_from(h, it, 1, batch_size, ns, &lr, nullptr);
+    if (rc == DE_OK && it < iterations - 1 && keep < h->dim) {
+      const cudaError_t e = launch_sparse_prune_f32(h->dim, h->d_x, h->n, keep, h->stream);
+      if (e != cudaSuccess) rc = cuda_fail(h, e, "launch_sparse_prune_f32");
+    }
+  }
+  drop_graph(h);
+  h->keep_last_edges = false;
+  if (rc) return rc;
+  h->sparse_in_mirror = true;
+  return DE_OK;
+}
+
+int de_sparse_get(de_handle *h, double *x, double *coll) {
+  if (!h || (!x && !coll)) return DE_ERR_INVALID;
+  if (!h->d_sx) return fail(h, DE_ERR_INVALID, "no sparse embedding rows: call de_sparse_set first");
+  DE_CUDA(h, cudaSetDevice(h->device));
+  const size_t count = size_t(h->n) * h->dim;
+  if (h->sparse_in_mirror) {
+    DE_CUDA(h, launch_f32_to_f64(h->d_x, h->d_sx, int64_t(count), h->stream));
+    h->sparse_in_mirror = false;
+  }
+  if (x) DE_CUDA(h, cudaMemcpyAsync(x, h->d_sx, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (coll) {
+    if (!h->d_coll || h->sparse_batch <= 0) return fail(h, DE_ERR_INVALID, "no batch collector: run first");
+    DE_CUDA(h, cudaMemcpyAsync(coll, h->d_coll, size_t(h->sparse_batch) * h->dim * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+  }
+  DE_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_device_error(h);
+}
+
+int de_sparse_embedding(de_handle *h, double *x, int32_t iterations, int32_t batch_size, int32_t ns, double lr,
+                        double density, int32_t merge, double *coll) {
+  if (!h || !x) return DE_ERR_INVALID;
+  int rc = de_sparse_set(h, x);
+  if (!rc) rc = de_sparse_run(h, iterations, batch_size, ns, lr, density, merge);
+  if (!rc) rc = de_sparse_get(h, x, coll);
+  return rc;
 }
 
 int de_sync(de_handle *h) {

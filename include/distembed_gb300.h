@@ -337,6 +337,37 @@ int de_spmm(de_handle *h, int32_t batch_size, double lr, double *y);
 /* The same into an FP32 n x dim buffer (a device pointer when on_device). */
 int de_spmm_f32(de_handle *h, int32_t batch_size, float lr, float *y, int32_t on_device);
 
+/* SparseEmbedding::algo_sparse_embedding(iterations, batch_size, ns, lr, density)
+ * at one rank (cpp/algo/sparse_embedding.hpp:78-194), which the driver runs for
+ * -sparse_embedding 1 (cpp/dist_embed.cpp:317-330).  x: host FP64 n x dim rows in
+ * the reference's dense-collector form, INT_MIN marking an absent entry
+ * (cpp/core/sparse_mat.hpp:367-377, 492-505); replaced by the rows after the
+ * run, absent entries as 0.  k = (int)(dim * density).
+ *   merge = 0: the reference's one-rank branch (lines 138-144).  The attractive
+ *     force on the union of two rows' present entries (lines 338-503) goes into
+ *     the batch collector, which that branch never merges: the values change
+ *     only by the top-k pruning after the first iteration (lines 172-186,
+ *     745-767).  coll (host FP64 batch_size x dim, may be NULL) receives the
+ *     collector: slot r summed over rows r, B + r, ... of every iteration.
+ *   merge = 1: per minibatch the repulsive pass on its negatives (lines 505-659),
+ *     the attractive pass, then merge_batch_collector (sparse_mat.hpp:385-400):
+ *     the steps of the multi-rank branch (lines 145-168) that touch the local
+ *     partition, with the repulsive row count of F8 under ref_quirks; the rows are
+ *     pruned to their k largest values after every iteration but the last.
+ * At equal values the pruning drops the lower dim first (the reference's heap
+ * order at ties is its own).  The handle's FP32 embedding becomes the rows'
+ * FP32 mirror (0 for an absent entry).  FP32 handles, dim 32, 64, 128 or 256. */
+int de_sparse_embedding(de_handle *h, double *x, int32_t iterations, int32_t batch_size, int32_t ns, double lr,
+                        double density, int32_t merge, double *coll);
+/* The same in three steps, the rows kept on the device between them:
+ * de_sparse_set copies x (host or device memory) in, de_sparse_run enqueues the run on the handle's
+ * stream (returns before it completes), de_sparse_get waits and copies the rows
+ * and/or the collector (either may be NULL). */
+int de_sparse_set(de_handle *h, const double *x);
+int de_sparse_run(de_handle *h, int32_t iterations, int32_t batch_size, int32_t ns, double lr, double density,
+                  int32_t merge);
+int de_sparse_get(de_handle *h, double *x, double *coll);
+
 /* The cudaStream_t the handle runs on (as void*). */
 void *de_stream(de_handle *h);
 
