@@ -357,18 +357,28 @@ class Handle:
     ABSENT = float(-2 ** 31)
 
     def sparse_embedding(self, x, iterations: int, batch_size: int, ns: int, lr: float, density: float,
-                         merge: bool = False):
+                         merge: bool = False, inplace: bool = False, coll=None):
         """The reference's sparse embedding at one rank (SparseEmbedding::algo_sparse_embedding,
         cpp/algo/sparse_embedding.hpp:78-194) on the handle's graph.  x: FP64 n x dim rows,
         Handle.ABSENT marking an absent entry.  Returns (rows after the run with absent
         entries as 0, batch collector [batch_size, dim]).  merge=False is the reference's
         one-rank branch (the collector is never merged; the rows change only by the top-k
         pruning); merge=True merges the collector into the rows after every minibatch,
-        with the repulsive pass first, as the multi-rank branch does."""
-        out = np.array(x, dtype=np.float64, order="C")
+        with the repulsive pass first, as the multi-rank branch does.  inplace=True
+        overwrites x (a C-contiguous FP64 array, e.g. pinned) instead of a copy; coll:
+        an FP64 [batch_size, dim] array to receive the collector."""
+        if inplace:
+            if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+                raise ValueError("inplace needs a C-contiguous FP64 array")
+            out = x
+        else:
+            out = np.array(x, dtype=np.float64, order="C")
         if out.shape != (self.n, self.dim):
             raise ValueError(f"x must be {self.n} x {self.dim}")
-        coll = np.zeros((batch_size, self.dim), dtype=np.float64)
+        if coll is None:
+            coll = np.zeros((batch_size, self.dim), dtype=np.float64)
+        elif coll.shape != (batch_size, self.dim) or coll.dtype != np.float64 or not coll.flags.c_contiguous:
+            raise ValueError(f"coll must be a C-contiguous FP64 {batch_size} x {self.dim} array")
         self._check(lib().de_sparse_embedding(self._h, out.ctypes.data, iterations, batch_size, ns, lr, density,
                                               int(merge), coll.ctypes.data))
         return out, coll

@@ -989,14 +989,17 @@ int de_sparse_run(de_handle *h, int32_t iterations, int32_t batch_size, int32_t 
     a.P = h->d_parts;
     a.counters = h->d_counters;
     a.bound = float(h->opt.max_bound);
+    // The rows change only by the pruning, so only the check after the first
+    // iteration can prune: after it floor(present / n) <= k, and the rows, hence
+    // the count, stay as they are.  The later checks are left out.
     for (int it = 0; it < iterations; ++it) {
       DE_CUDA(h, launch_sparse_attract(h->dim, a, h->stream));
       DE_CUDA(h, launch_sparse_collect(h->d_y, h->d_coll, h->n, batch_size, h->dim, h->stream));
-      if (it < iterations - 1) {
+      if (it == 0 && iterations > 1) {
         DE_CUDA(h, cudaMemsetAsync(h->d_present, 0, sizeof(unsigned long long), h->stream));
         DE_CUDA(h, launch_sparse_count(h->d_sx, count, h->d_present, h->stream));
         DE_CUDA(h, launch_sparse_prune_f64(h->dim, h->d_sx, h->d_x, h->n, keep, h->d_present, h->stream));
-      } else {
+      } else if (it == iterations - 1) {
         DE_CUDA(h, launch_sparse_finalize(h->d_sx, count, h->stream));
       }
     }

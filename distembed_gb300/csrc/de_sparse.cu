@@ -95,8 +95,19 @@ __global__ void __launch_bounds__(256)
   const int64_t slots = int64_t(batch) * dim;
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < slots; e += int64_t(gridDim.x) * blockDim.x) {
     const int64_t r = e / dim;
+    const float *yp = y + r * dim + (e - r * dim);
+    const int64_t stride = int64_t(batch) * dim;
+    const int64_t rows = (n - r + batch - 1) / batch;  // rows r, r + B, ... below n
     double c = coll[e];
-    for (int64_t row = r; row < n; row += batch) c += double(__ldg(y + row * dim + (e - r * dim)));
+    int64_t q = 0;
+    for (; q + 8 <= rows; q += 8) {  // eight loads in flight, added in order
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldg(yp + (q + u) * stride);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) c += double(v[u]);
+    }
+    for (; q < rows; ++q) c += double(__ldg(yp + q * stride));
     coll[e] = c;
   }
 }
@@ -143,11 +154,13 @@ __device__ __forceinline__ uint64_t order_key(float v) {
 
 // Top-k pruning (preserveHighestK, sparse_embedding.hpp:745-767): in every row
 // the dim - keep smallest values become absent; at equal values the lower dim
-// goes first.  One warp per row; lane l holds dims l, l + 32, ...; the rank of
-// a value is the count of the row's values ordered before it.  T = double: the
-// FP64 rows (absent = INT_MIN) and their mirror; T = float: the mirror alone.
-// With `present` set the rows are pruned only when floor(present / n) > keep
-// (sparse_embedding.hpp:172-181), decided here so that the host need not wait.
+// goes first.  One warp per row, lane l holding dims [lN, lN + N): a bitonic
+// sort of the row's (key, dim) pairs in registers (partners across lanes by
+// shuffle, within a lane directly), after which sorted position p < dim - keep
+// names a dim to drop.  T = double: the FP64 rows (absent = INT_MIN) and their
+// mirror; T = float: the mirror alone.  With `present` set the rows are pruned
+// only when floor(present / n) > keep (sparse_embedding.hpp:172-181), decided
+// here so that the host need not wait.
 template <int D, typename T>
 __global__ void __launch_bounds__(256) sparse_prune_kernel(T *xs, float *x32, int64_t n, int32_t keep,
                                                            const unsigned long long *present) {
@@ -159,29 +172,48 @@ __global__ void __launch_bounds__(256) sparse_prune_kernel(T *xs, float *x32, in
        row += int64_t(gridDim.x) * (blockDim.x >> 5)) {
     T *xr = xs + row * D;
     uint64_t key[N];
-    int rank[N];
+    int idx[N];
 #pragma unroll
     for (int t = 0; t < N; ++t) {
-      key[t] = order_key(xr[lane + 32 * t]);
-      rank[t] = 0;
+      idx[t] = lane * N + t;
+      key[t] = order_key(xr[idx[t]]);
     }
 #pragma unroll
-    for (int tb = 0; tb < N; ++tb) {
-      for (int src = 0; src < 32; ++src) {
-        const uint64_t kb = __shfl_sync(kFull, key[tb], src);
-        const int db = src + 32 * tb;
+    for (int k = 2; k <= D; k <<= 1) {
 #pragma unroll
-        for (int t = 0; t < N; ++t) rank[t] += (kb < key[t]) || (kb == key[t] && db < lane + 32 * t);
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        uint64_t pk[N];
+        int pi[N];
+#pragma unroll
+        for (int t = 0; t < N; ++t) {
+          if (j >= N) {
+            pk[t] = __shfl_xor_sync(kFull, key[t], j / N);
+            pi[t] = __shfl_xor_sync(kFull, idx[t], j / N);
+          } else {
+            pk[t] = key[t ^ j];
+            pi[t] = idx[t ^ j];
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < N; ++t) {
+          const int i = lane * N + t;
+          const bool keep_min = ((i & j) == 0) == ((i & k) == 0);
+          const bool p_less = pk[t] < key[t] || (pk[t] == key[t] && pi[t] < idx[t]);
+          if (keep_min == p_less) {
+            key[t] = pk[t];
+            idx[t] = pi[t];
+          }
+        }
       }
     }
 #pragma unroll
     for (int t = 0; t < N; ++t)
-      if (rank[t] < nullify) {
+      if (lane * N + t < nullify) {
         if constexpr (sizeof(T) == 8) {
-          xr[lane + 32 * t] = __longlong_as_double(int64_t(kAbsent64));
-          x32[row * D + lane + 32 * t] = 0.f;
+          xr[idx[t]] = __longlong_as_double(int64_t(kAbsent64));
+          x32[row * D + idx[t]] = 0.f;
         } else {
-          xr[lane + 32 * t] = 0.f;  // xs is the mirror itself
+          xr[idx[t]] = 0.f;  // xs is the mirror itself
         }
       }
   }

@@ -9,9 +9,13 @@
 // at compile time), -precision fp32|bf16, -device, -csr gpu|host.  -spmm 1 runs
 // the reference's SpMM baseline instead (BaselineSpMM::execute,
 // cpp/algo/baseline_spmm.hpp:52-90: per iteration a fresh DenseMat and one
-// SpMMAlgo::algo_spmm step, timed).  Flags that select the other algorithms of
-// the reference (-spgemm, -sparse_embedding, -msbfs) are refused; flags of the
-// multi-rank exchange are accepted and not used.
+// SpMMAlgo::algo_spmm step, timed).  -sparse_embedding 1 runs the reference's
+// sparse embedding (cpp/dist_embed.cpp:317-330: an SpMat of rand() rows,
+// SparseEmbedding::algo_sparse_embedding(iterations, batch, ns, lr, density), its
+// rows written as embedding.txt) with -density (default 0.5) and the extra flag
+// -sparse_merge 1 (merge the batch collector after every minibatch).  Flags that
+// select the other algorithms of the reference (-spgemm, -msbfs) are refused;
+// flags of the multi-rank exchange are accepted and not used.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -48,6 +52,9 @@ struct Flags {
   bool col_major = false, sync_comm = false;
   bool gpu_csr = true;  // -csr gpu|host: where the input's COO -> CSR runs
   bool spmm = false;    // -spmm 1: the SpMM baseline (cpp/dist_embed.cpp:255-268)
+  bool sparse = false;  // -sparse_embedding 1 (cpp/dist_embed.cpp:317-330)
+  bool sparse_merge = false;
+  double density = 0.5;  // cpp/dist_embed.cpp:62
   int precision = DE_PRECISION_FP32;
 };
 
@@ -100,6 +107,45 @@ int run_spmm(const Flags &f, const CSRHandle &csr, int64_t rows, int64_t nnz) {
   return 0;
 }
 
+// The -sparse_embedding branch at one rank (cpp/dist_embed.cpp:317-330): the
+// output SpMat's rows from rand() (sparse_mat.hpp:367-377, row-major, the same
+// draws as DenseMat's), the sparse embedding, its rows written by parallel_write.
+int run_sparse(const Flags &f, const CSRHandle &csr, int64_t rows, int64_t nnz) {
+  de_options o;
+  de_default_options(&o);
+  o.device = f.device;
+  de_handle *h = nullptr;
+  if (de_create(rows, csr.rowStart.data(), csr.col_idx.data(), nnz, f.dim, &o, &h) != DE_OK) {
+    std::fprintf(stderr, "sparse_embedding: %s\n", de_last_error(nullptr));
+    return 1;
+  }
+  std::vector<double> x(size_t(rows) * size_t(f.dim));
+  for (double &v : x) v = -1.0 + 2.0 * std::rand() / (RAND_MAX + 1.0);
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = de_sparse_embedding(h, x.data(), f.iterations, f.batch_size, f.ns, f.lr, f.density,
+                                     f.sparse_merge ? 1 : 0, nullptr);
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rc != DE_OK) {
+    std::fprintf(stderr, "sparse_embedding: %s\n", de_last_error(h));
+    de_destroy(h);
+    return 1;
+  }
+  de_destroy(h);
+  std::printf(" rank 0 sparse embedding completed in %.3f s\n", secs);
+  const std::string out = f.output + "/embedding.txt";
+  if (de_embedding_write(out.c_str(), x.data(), rows, f.dim) != DE_OK) {
+    std::fprintf(stderr, "writing %s: %s\n", out.c_str(), de_last_error(nullptr));
+    return 1;
+  }
+  if (FILE *pf = std::fopen("perf_output", "a")) {
+    std::fprintf(pf, "{\"algo\":\"SparseEmbedding\",\"p\":1,\"data_set\":\"%s\",\"device\":\"GB300\","
+                     "\"total_time_s\":%.6f,\"iterations\":%d,\"batch\":%d,\"density\":%g,\"merge\":%d}\n",
+                 f.dataset.c_str(), secs, f.iterations, f.batch_size, f.density, f.sparse_merge ? 1 : 0);
+    std::fclose(pf);
+  }
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -122,9 +168,12 @@ int main(int argc, char **argv) {
     else if (!std::strcmp(a, "-csr")) f.gpu_csr = std::strcmp(v, "host") != 0;
     else if (!std::strcmp(a, "-precision")) f.precision = std::strcmp(v, "bf16") ? DE_PRECISION_FP32 : DE_PRECISION_BF16;
     else if (!std::strcmp(a, "-spmm")) f.spmm = std::atoi(v) == 1;
-    else if ((!std::strcmp(a, "-spgemm") || !std::strcmp(a, "-sparse_embedding") || !std::strcmp(a, "-msbfs")) &&
-             std::atoi(v) == 1) {
-      std::fprintf(stderr, "%s: only the force-model embedding and the SpMM baseline are provided by this build\n", a);
+    else if (!std::strcmp(a, "-sparse_embedding")) f.sparse = std::atoi(v) == 1;
+    else if (!std::strcmp(a, "-sparse_merge")) f.sparse_merge = std::atoi(v) == 1;
+    else if (!std::strcmp(a, "-density")) f.density = std::atof(v);
+    else if ((!std::strcmp(a, "-spgemm") || !std::strcmp(a, "-msbfs")) && std::atoi(v) == 1) {
+      std::fprintf(stderr, "%s: only the force-model embedding, the SpMM baseline and the sparse embedding are "
+                           "provided by this build\n", a);
       return 2;
     }
   }
@@ -173,6 +222,7 @@ int main(int argc, char **argv) {
   sp.gNNz = nnz;
   std::printf(" rank 0 gROWs  %lld gCols %lld nnz %lld\n", (long long)rows, (long long)cols, (long long)nnz);
   if (f.spmm) return run_spmm(f, csr, rows, nnz);
+  if (f.sparse) return run_sparse(f, csr, rows, nnz);
   // ---- initial embedding (cpp/core/dense_mat.hpp:55-63)
   std::vector<double> coords(size_t(rows) * size_t(f.dim));
   for (size_t i = 0; i < coords.size(); ++i) coords[i] = -1.0 + 2.0 * std::rand() / (RAND_MAX + 1.0);

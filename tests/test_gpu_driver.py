@@ -100,3 +100,26 @@ def test_driver_spmm_baseline(tmp_path):
     line = [ln for ln in open(tmp_path / "perf_output") if '"SpMM"' in ln][-1]
     import json
     assert len(json.loads(line)["iteration_time_s"]) == 3
+
+
+@pytest.mark.parametrize("merge", ["0", "1"])
+def test_driver_sparse_embedding(tmp_path, merge):
+    """-sparse_embedding 1: the reference's sparse embedding branch
+    (cpp/dist_embed.cpp:317-330): rand() rows, algo_sparse_embedding, embedding.txt."""
+    n, rp, col = gg.knn_csr(900, 8, 6, 3, seed=9)
+    mtx = str(tmp_path / "g.mtx")
+    gg.write_mtx(mtx, n, rp, col)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([de.DRIVER_PATH, "-input", mtx, "-output", str(out), "-sparse_embedding", "1", "-iter", "3",
+                        "-batch", "128", "-dim", "64", "-lr", "0.02", "-density", "0.5", "-sparse_merge", merge],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    ids, x = read_embedding(str(out / "embedding.txt"), 64)
+    assert np.array_equal(ids, np.arange(1, n + 1))
+    xo, _ = oracle.sparse_embedding(rp, col, reference_init(n, 64), 3, 128, 5, 0.02, 0.5, merge=merge == "1")
+    assert np.max(np.abs(x - xo)) <= 6e-6 + (1e-4 if merge == "1" else 0.0)
+    if merge == "0":
+        assert np.all((x != 0).sum(1) == 32)
+    line = [ln for ln in open(tmp_path / "perf_output") if '"SparseEmbedding"' in ln][-1]
+    assert '"iterations":3' in line

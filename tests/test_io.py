@@ -79,6 +79,9 @@ def test_driver_usage_and_missing_input_without_a_gpu(tmp_path):
     assert r.returncode == 2
     r = subprocess.run([exe, "-input", str(tmp_path / "none.mtx"), "-spmm", "1"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+    r = subprocess.run([exe, "-input", str(tmp_path / "none.mtx"), "-sparse_embedding", "1"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
 
 
 def test_cpp_header_compiles_against_reference_shaped_types(tmp_path):
