@@ -88,7 +88,11 @@ __global__ void __launch_bounds__(kWarps * 32) sparse_attract_kernel(const SpmmA
 // Batch collector: slot r of minibatch j holds row jB + r, and the one-rank
 // branch adds every minibatch into the same slots without clearing them
 // (sparse_embedding.hpp:452-455, 380-386): coll[r] += Y[r] + Y[B + r] + ..., in
-// minibatch order, in FP64.
+// minibatch order.  The terms are FP32 (the rows' updates); their running sum is
+// kept as an unevaluated FP32 pair hi + lo (Knuth's TwoSum adds each term with
+// its rounding error carried in lo, about 44 bits of precision), then added to
+// the FP64 collector once: two FP64 operations per slot instead of two per term
+// on the GPU's narrow FP64 pipe.
 __global__ void __launch_bounds__(256)
     sparse_collect_kernel(const float *__restrict__ y, double *__restrict__ coll, int64_t n, int32_t batch,
                           int32_t dim) {
@@ -98,17 +102,24 @@ __global__ void __launch_bounds__(256)
     const float *yp = y + r * dim + (e - r * dim);
     const int64_t stride = int64_t(batch) * dim;
     const int64_t rows = (n - r + batch - 1) / batch;  // rows r, r + B, ... below n
-    double c = coll[e];
+    float hi = 0.f, lo = 0.f;
+    auto add = [&](float v) {
+      const float s = __fadd_rn(hi, v);
+      const float bv = __fsub_rn(s, hi);
+      const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(v, bv));
+      hi = s;
+      lo = __fadd_rn(lo, err);
+    };
     int64_t q = 0;
     for (; q + 8 <= rows; q += 8) {  // eight loads in flight, added in order
       float v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) v[u] = __ldg(yp + (q + u) * stride);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) c += double(v[u]);
+      for (int u = 0; u < 8; ++u) add(v[u]);
     }
-    for (; q < rows; ++q) c += double(__ldg(yp + q * stride));
-    coll[e] = c;
+    for (; q < rows; ++q) add(__ldg(yp + q * stride));
+    coll[e] = coll[e] + (double(hi) + double(lo));
   }
 }
 
