@@ -32,7 +32,7 @@ int elementwise_grid(int64_t count) { return int(count / 256 + 1 < 152 * 8 ? cou
 // iteration): one warp per work item, U neighbours in flight, split rows
 // combined in piece order.  Row i's update goes to Y[i] (FP32, from zero).
 template <int D, int U>
-__global__ void __launch_bounds__(kWarps * 32) sparse_attract_kernel(const SpmmArgs a) {
+__global__ void __launch_bounds__(kWarps * 32, D == 128 ? 5 : 1) sparse_attract_kernel(const SpmmArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = blockIdx.x * int64_t(kWarps) + (threadIdx.x >> 5);
   if (gw >= a.n_items) return;
