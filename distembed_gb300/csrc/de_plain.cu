@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
 // work item, U rows in flight; split rows are combined in piece order as in
 // plain_batch_kernel.
 template <int D, int U>
-__global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBlocks)
+__global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : (D == 128 ? 10 : kPlainMinBlocks))
     spmm_kernel(const SpmmArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = blockIdx.x * int64_t(kPlainWarps) + (threadIdx.x >> 5);
