@@ -168,7 +168,9 @@ __device__ __forceinline__ uint64_t order_key(float v) {
 // goes first.  One warp per row, lane l holding dims [lN, lN + N): a bitonic
 // sort of the row's (key, dim) pairs in registers (partners across lanes by
 // shuffle, within a lane directly), after which sorted position p < dim - keep
-// names a dim to drop.  T = double: the FP64 rows (absent = INT_MIN) and their
+// names a dim to drop.  When half the row is dropped (density 0.5) the first
+// step of the last merge already puts the D/2 smallest pairs below position
+// D/2, and the remaining steps, which only order the halves, are skipped.  T = double: the FP64 rows (absent = INT_MIN) and their
 // mirror; T = float: the mirror alone.  With `present` set the rows are pruned
 // only when floor(present / n) > keep (sparse_embedding.hpp:172-181), decided
 // here so that the host need not wait.
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(256) sparse_prune_kernel(T *xs, float *x32, in
             idx[t] = pi[t];
           }
         }
+        if (k == D && j == D / 2 && nullify == D / 2) break;
       }
     }
 #pragma unroll
