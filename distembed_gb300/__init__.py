@@ -433,8 +433,11 @@ class EmbeddingAlgo:
     reference, algo_force2_vec_ns updates it in place.  The CSR is the native
     matrix's (rowStart, col_idx).  alpha, beta and sync_comm steer the
     multi-rank exchange, which a single resident partition does not have; they
-    are accepted and ignored.  col_major selects the reference's transposed
-    attractive traversal, which is not provided (it raises).
+    are accepted and ignored.  col_major makes the passes read the receiver
+    matrix's CSR, the transpose of the native one, as the reference's loop does
+    (cpp/algo/algo.hpp:131-133; at one rank it then runs the row-major pass,
+    :184-186): on an asymmetric graph each row takes its attractive forces from
+    its in-neighbours.
     """
 
     def __init__(self, rowptr, col, dense: np.ndarray, alpha: float = 0.0, beta: float = 0.25,
@@ -442,7 +445,8 @@ class EmbeddingAlgo:
                  sync_comm: bool = False, *, quirks: bool = True, precision: str = "fp32",
                  device: int = 0, stream: int | None = None, compute_loss: bool = True):
         if col_major:
-            raise DEError(DE_ERR_UNSUPPORTED, "col_major traversal is not provided")
+            from .graphgen import transpose_csr
+            rowptr, col = transpose_csr(rowptr, col, dense.shape[0])
         if min_bound != -max_bound:
             raise DEError(DE_ERR_INVALID, "the reference clips to [-MAX_BOUND, MAX_BOUND]")
         if dense.dtype != np.float64 or dense.ndim != 2 or not dense.flags.c_contiguous:

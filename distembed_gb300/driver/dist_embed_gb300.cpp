@@ -58,11 +58,27 @@ struct Flags {
   int precision = DE_PRECISION_FP32;
 };
 
+// The receiver matrix's CSR: the transpose of the native one (cpp/dist_embed.cpp:197-200,
+// CSRLocal with transpose = true), columns ascending in each row; it has `cols` rows.
+void transpose_csr(const CSRHandle &a, int64_t rows, int64_t cols, CSRHandle &t) {
+  const int64_t nnz = a.rowStart[size_t(rows)];
+  t.rowStart.assign(size_t(cols) + 1, 0);
+  t.col_idx.assign(size_t(nnz > 0 ? nnz : 1), 0);
+  for (int64_t e = 0; e < nnz; ++e) t.rowStart[size_t(a.col_idx[size_t(e)]) + 1]++;
+  for (int64_t c = 0; c < cols; ++c) t.rowStart[size_t(c) + 1] += t.rowStart[size_t(c)];
+  std::vector<int64_t> fill(t.rowStart.begin(), t.rowStart.end() - 1);
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t e = a.rowStart[size_t(r)]; e < a.rowStart[size_t(r) + 1]; ++e)
+      t.col_idx[size_t(fill[size_t(a.col_idx[size_t(e)])]++)] = r;
+}
+
 template <size_t D>
-double run(const Flags &f, SpMat &sp, DenseMat &dense, std::vector<double> &loss) {
+double run(const Flags &f, SpMat &sp, SpMat &receiver, DenseMat &dense, std::vector<double> &loss) {
   Grid grid;
-  distembed_gb300::GpuEmbeddingAlgo<int64_t, double, D> algo(&sp, &sp, &sp, &dense, &grid, f.alpha, f.beta, 5.0, -5.0,
-                                                             f.col_major, f.sync_comm, f.precision, f.device);
+  // with -col_major 1 the passes read the receiver's CSR (cpp/algo/algo.hpp:131-133)
+  distembed_gb300::GpuEmbeddingAlgo<int64_t, double, D> algo(&sp, &receiver, &sp, &dense, &grid, f.alpha, f.beta,
+                                                             5.0, -5.0, f.col_major, f.sync_comm, f.precision,
+                                                             f.device);
   const auto t0 = std::chrono::steady_clock::now();
   algo.algo_force2_vec_ns(f.iterations, f.batch_size, f.ns, f.lr);
   const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -230,14 +246,17 @@ int main(int argc, char **argv) {
   dense.rows = uint64_t(rows);
   dense.nCoordinates = coords.data();
   // ---- the algorithm (cpp/dist_embed.cpp:331-344)
+  SpMat receiver;
+  if (f.col_major) transpose_csr(csr, rows, cols, *receiver.csr_local_data->handler);
+  SpMat &rec = f.col_major ? receiver : sp;
   std::vector<double> loss;
   double secs = 0;
   try {
     switch (f.dim) {
-      case 32: secs = run<32>(f, sp, dense, loss); break;
-      case 64: secs = run<64>(f, sp, dense, loss); break;
-      case 128: secs = run<128>(f, sp, dense, loss); break;
-      case 256: secs = run<256>(f, sp, dense, loss); break;
+      case 32: secs = run<32>(f, sp, rec, dense, loss); break;
+      case 64: secs = run<64>(f, sp, rec, dense, loss); break;
+      case 128: secs = run<128>(f, sp, rec, dense, loss); break;
+      case 256: secs = run<256>(f, sp, rec, dense, loss); break;
       default: std::fprintf(stderr, "-dim must be 32, 64, 128 or 256\n"); return 2;
     }
   } catch (const distembed_gb300::Error &e) {

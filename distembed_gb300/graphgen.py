@@ -34,6 +34,17 @@ def coo_to_csr(n: int, src: np.ndarray, dst: np.ndarray, dedup: bool = True):
     return rowptr, col
 
 
+def transpose_csr(rowptr, col, n: int | None = None):
+    """The CSR of the transposed matrix (columns ascending in each row): the
+    receiver matrix's CSR, which the reference's col_major flag selects
+    (cpp/algo/algo.hpp:131-133, built with transpose = true, cpp/dist_embed.cpp:197-200)."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    n = len(rowptr) - 1 if n is None else n
+    src = np.repeat(np.arange(len(rowptr) - 1, dtype=np.int64), np.diff(rowptr))
+    return coo_to_csr(n, col, src, dedup=False)
+
+
 def symmetrise(src, dst, drop_self_loops: bool = True):
     s = np.concatenate([src, dst])
     d = np.concatenate([dst, src])

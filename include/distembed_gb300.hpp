@@ -14,10 +14,13 @@
  * and writes the embedding back in place, as the reference does.  receiver,
  * sender, grid, alpha, beta and sync_comm steer the multi-rank exchange, which
  * one resident partition does not have: they are accepted and not used.
- * col_major is accepted and does not change the result: the reference's one-rank
- * branch calls the attractive pass with col_major = false whatever the flag
- * (cpp/algo/algo.hpp:184-186); the transposed traversal (algo.hpp:450-518) runs
- * only in the multi-rank exchange.
+ * col_major selects the CSR the passes read, as the reference's loop does
+ * (cpp/algo/algo.hpp:131-133): the receiver matrix's, built with transpose = true
+ * (cpp/dist_embed.cpp:197-200), so on an asymmetric graph a row takes its
+ * attractive forces from its in-neighbours.  The traversal stays the row-major
+ * one: the one-rank branch calls the attractive pass with col_major = false
+ * whatever the flag (algo.hpp:184-186); the transposed traversal (algo.hpp:450-518,
+ * racy in the reference) runs only in the multi-rank exchange.
  *
  * Errors throw distembed_gb300::Error (a std::runtime_error) with the library's
  * message, where the reference prints and exits.
@@ -25,6 +28,7 @@
 #ifndef DISTEMBED_GB300_HPP
 #define DISTEMBED_GB300_HPP
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <stdexcept>
@@ -57,12 +61,16 @@ class GpuEmbeddingAlgo {
  public:
   /* The reference constructor (cpp/algo/algo.hpp:54-63). */
   template <class SpMat, class DenseMat, class Grid>
-  GpuEmbeddingAlgo(SpMat *native, SpMat * /*receiver*/, SpMat * /*sender*/, DenseMat *dense, Grid * /*grid*/,
+  GpuEmbeddingAlgo(SpMat *native, SpMat *receiver, SpMat * /*sender*/, DenseMat *dense, Grid * /*grid*/,
                    double /*alpha*/, double /*beta*/, VALUE_TYPE MAX_BOUND, VALUE_TYPE MIN_BOUND, bool col_major,
                    bool /*sync_comm*/, int precision = DE_PRECISION_FP32, int device = 0) {
-    const auto &csr = *native->csr_local_data->handler;
+    const auto &csr = col_major ? *receiver->csr_local_data->handler : *native->csr_local_data->handler;
     const int64_t n = int64_t(dense->rows);
-    std::vector<int64_t> rowptr(csr.rowStart.begin(), csr.rowStart.begin() + (n + 1));
+    // a transposed CSR of a matrix with fewer columns than rows has fewer row
+    // pointers: the rows past them have no entries
+    const int64_t have = std::min<int64_t>(int64_t(csr.rowStart.size()), n + 1);
+    std::vector<int64_t> rowptr(csr.rowStart.begin(), csr.rowStart.begin() + have);
+    rowptr.resize(size_t(n + 1), have > 0 ? rowptr[size_t(have - 1)] : 0);
     std::vector<int64_t> col(csr.col_idx.begin(), csr.col_idx.begin() + rowptr[n]);
     init(n, rowptr.data(), col.data(), dense->nCoordinates, MAX_BOUND, MIN_BOUND, col_major, precision, device);
   }
@@ -104,7 +112,7 @@ class GpuEmbeddingAlgo {
  private:
   void init(int64_t n, const int64_t *rowptr, const int64_t *col, VALUE_TYPE *coordinates, VALUE_TYPE max_bound,
             VALUE_TYPE min_bound, bool col_major, int precision, int device) {
-    (void)col_major;  // one rank: the row-major pass whatever the flag (algo.hpp:184-186)
+    (void)col_major;  // the CSR was chosen by the caller; the pass is row-major (algo.hpp:184-186)
     if (min_bound != -max_bound) throw Error(DE_ERR_INVALID, "the bounds must be [-MAX_BOUND, MAX_BOUND]");
     de_options o;
     de_default_options(&o);

@@ -76,7 +76,7 @@ def ref():
     if _REF is None:
         L = ctypes.CDLL(ref_path())
         L.deref_run.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p,
-                                ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int]
+                                ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, ctypes.c_int]
         L.deref_batch_grad.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i64p, _i64p, _f64p,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, _f64p]
@@ -169,15 +169,16 @@ def ref_negatives(lower: int, upper: int, seed: int, ns: int) -> np.ndarray:
     return out[:ns]
 
 
-def ref_run(rowptr, col, x, epochs, batch, ns, lr, driver_loop=False):
-    """The reference's EmbeddingAlgo (FP64, its quirks included).  Returns x_new,
-    or None when a negative draw would hit the reference's undefined path."""
+def ref_run(rowptr, col, x, epochs, batch, ns, lr, driver_loop=False, col_major=False):
+    """The reference's EmbeddingAlgo (FP64, its quirks included; col_major as its
+    constructor flag).  Returns x_new, or None when a negative draw would hit the
+    reference's undefined path."""
     rowptr, col = _csr(rowptr, col)
     x = np.array(x, dtype=np.float64, order="C", copy=True)
     n, dim = x.shape
     lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
     rc = ref().deref_run(dim, n, len(col), _p(rowptr, _i64p), _p(col, _i64p), _p(x, _f64p), epochs,
-                         batch, ns, _p(lrs, _f64p), int(driver_loop))
+                         batch, ns, _p(lrs, _f64p), int(driver_loop), int(col_major))
     if rc == -2:
         return None
     if rc != 0:

@@ -69,7 +69,7 @@ bool draws_in_range(int64_t n, int epochs, int batches, int ns) {
 
 template <size_t D>
 int run_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, double *emb,
-            int epochs, int batch, int ns, const double *lr, int use_driver_loop) {
+            int epochs, int batch, int ns, const double *lr, int use_driver_loop, int col_major) {
   int batches = int(n / batch) + (n % batch ? 1 : 0);
   // A draw equal to gRows makes the reference index a one-element cache
   // vector out of range (cpp/algo/algo.hpp:605-617 at one rank): undefined
@@ -80,7 +80,7 @@ int run_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, d
   std::memcpy(dense.nCoordinates, emb, sizeof(double) * size_t(n) * D);
   distblas::algo::EmbeddingAlgo<INDEX_TYPE, double, D> algo(
       g.native.get(), g.receiver.get(), g.sender.get(), &dense, &g.grid, 0.0, 0.25, 5, -5,
-      false, false);
+      col_major != 0, false);
   if (use_driver_loop) {
     // The reference's own epoch/minibatch loop (cpp/algo/algo.hpp:74-262);
     // it takes one constant learning rate.
@@ -90,7 +90,9 @@ int run_dim(int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col, d
     // The one-rank branch of that loop (cpp/algo/algo.hpp:164-192) with a
     // learning rate per epoch.
     int last_batch_size = (n % batch) ? int(n - int64_t(batch) * (batches - 1)) : batch;
-    CSRLocal<double> *csr_block = g.native->csr_local_data.get();
+    // the CSR the loop reads: the receiver's (transposed) one with col_major
+    // (cpp/algo/algo.hpp:131-133)
+    CSRLocal<double> *csr_block = col_major ? g.receiver->csr_local_data.get() : g.native->csr_local_data.get();
     vector<double> prev(size_t(batch) * D);
     int considering_batch_size = batch;
     for (int i = 0; i < epochs; ++i) {
@@ -235,17 +237,18 @@ int deref_spmm(int dim, int64_t n, int64_t nnz, const int64_t *rowptr, const int
 
 /* Runs `epochs` epochs of the reference embedding step in place on emb (n x dim,
  * row-major FP64).  lr holds one rate per epoch; use_driver_loop = 1 calls
- * algo_force2_vec_ns itself (lr[0] only).  Returns 0, -1 for an unsupported
- * dim, -2 when a negative draw would hit the reference's out-of-range path. */
+ * algo_force2_vec_ns itself (lr[0] only); col_major is the constructor's flag.
+ * Returns 0, -1 for an unsupported dim, -2 when a negative draw would hit the
+ * reference's out-of-range path. */
 int deref_run(int dim, int64_t n, int64_t nnz, const int64_t *rowptr, const int64_t *col,
               double *emb, int epochs, int batch, int ns, const double *lr,
-              int use_driver_loop) {
+              int use_driver_loop, int col_major) {
   switch (dim) {
-    case 16: return run_dim<16>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop);
-    case 32: return run_dim<32>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop);
-    case 64: return run_dim<64>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop);
-    case 128: return run_dim<128>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop);
-    case 256: return run_dim<256>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop);
+    case 16: return run_dim<16>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop, col_major);
+    case 32: return run_dim<32>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop, col_major);
+    case 64: return run_dim<64>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop, col_major);
+    case 128: return run_dim<128>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop, col_major);
+    case 256: return run_dim<256>(n, nnz, rowptr, col, emb, epochs, batch, ns, lr, use_driver_loop, col_major);
   }
   return -1;
 }

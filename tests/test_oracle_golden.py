@@ -145,3 +145,25 @@ def test_oracle_sparse_embedding_matches_reference_live(merge):
             continue
         got = oracle.sparse_embedding(rp, col, x, iters, batch, 5, 0.05, density, merge)
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference harness is only buildable where its sources are")
+def test_col_major_reads_the_transposed_csr():
+    # with col_major the reference's loop reads the receiver matrix's CSR, the
+    # transpose of the native one (cpp/algo/algo.hpp:131-133), and runs the row-major
+    # pass on it (:184-186): on a directed graph, the oracle on the transposed CSR
+    from distembed_gb300 import graphgen as gg
+    n = 600
+    rng = np.random.default_rng(41)
+    src, dst = rng.integers(0, n, 5000), rng.integers(0, n, 5000)
+    keep = src != dst
+    rp, col = gg.coo_to_csr(n, src[keep], dst[keep])
+    trp, tcol = gg.transpose_csr(rp, col)
+    x0 = gg.init_embedding(n, 32, 42)
+    for driver in (True, False):
+        xr = oracle.ref_run(rp, col, x0, 3, 128, 5, 0.03, driver_loop=driver, col_major=True)
+        if xr is None:
+            pytest.skip("draw hits the reference's undefined path")
+        xo, _ = oracle.run(trp, tcol, x0, 3, 128, 5, 0.03, quirks=True)
+        assert np.array_equal(xr, xo)
+        assert not np.array_equal(xr, oracle.ref_run(rp, col, x0, 3, 128, 5, 0.03, driver_loop=driver))
