@@ -381,6 +381,7 @@ class Handle:
             raise ValueError(f"coll must be a C-contiguous FP64 {batch_size} x {self.dim} array")
         self._check(lib().de_sparse_embedding(self._h, out.ctypes.data, iterations, batch_size, ns, lr, density,
                                               int(merge), coll.ctypes.data))
+        self._sparse_batch = batch_size
         return out, coll
 
     def sparse_set(self, x):
@@ -400,11 +401,15 @@ class Handle:
                    merge: bool = False):
         """Enqueue a sparse embedding run on the device-resident rows (returns at once)."""
         self._check(lib().de_sparse_run(self._h, iterations, batch_size, ns, lr, density, int(merge)))
+        self._sparse_batch = batch_size
 
-    def sparse_get(self, batch_size: int = 0):
-        """Wait for the run and return (rows, batch collector or None)."""
+    def sparse_get(self, collector: bool = True):
+        """Wait for the run and return (rows, batch collector of the last run, or None)."""
         x = np.empty((self.n, self.dim), dtype=np.float64)
-        coll = np.empty((batch_size, self.dim), dtype=np.float64) if batch_size > 0 else None
+        batch = getattr(self, "_sparse_batch", 0)
+        if collector and batch <= 0:
+            raise DEError(DE_ERR_INVALID, "no batch collector: run first")
+        coll = np.empty((batch, self.dim), dtype=np.float64) if collector else None
         self._check(lib().de_sparse_get(self._h, x.ctypes.data, coll.ctypes.data if coll is not None else None))
         return x, coll
 

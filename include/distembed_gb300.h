@@ -362,7 +362,8 @@ int de_sparse_embedding(de_handle *h, double *x, int32_t iterations, int32_t bat
 /* The same in three steps, the rows kept on the device between them:
  * de_sparse_set copies x (host or device memory) in, de_sparse_run enqueues the run on the handle's
  * stream (returns before it completes), de_sparse_get waits and copies the rows
- * and/or the collector (either may be NULL). */
+ * (n x dim) and/or the collector (the last run's batch_size x dim); either may
+ * be NULL. */
 int de_sparse_set(de_handle *h, const double *x);
 int de_sparse_run(de_handle *h, int32_t iterations, int32_t batch_size, int32_t ns, double lr, double density,
                   int32_t merge);

@@ -107,7 +107,7 @@ def test_three_step_api_equals_one_call():
         one_x, one_c = h.sparse_embedding(x, 3, 512, 5, 0.05, 0.5)
         h.sparse_set(x)
         h.sparse_run(3, 512, 5, 0.05, 0.5)
-        three_x, three_c = h.sparse_get(512)
+        three_x, three_c = h.sparse_get()
     assert np.array_equal(one_x, three_x) and np.array_equal(one_c, three_c)
 
 
