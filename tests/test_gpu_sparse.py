@@ -65,7 +65,7 @@ def test_one_rank_branch_matches_oracle(dim, kind, iterations, density):
         assert np.all((got_x != 0).sum(1) == int(dim * density))
 
 
-@pytest.mark.parametrize("dim", [32, 128])
+@pytest.mark.parametrize("dim", [32, 64, 128, 256])
 @pytest.mark.parametrize("kind", ["rmat", "knn"])
 @pytest.mark.parametrize("quirks", [True, False])
 def test_merge_matches_oracle(dim, kind, quirks):
