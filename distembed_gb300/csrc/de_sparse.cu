@@ -30,7 +30,9 @@ int elementwise_grid(int64_t count) { return int(count / 256 + 1 < 152 * 8 ? cou
 // The attractive pass of every minibatch of one iteration in one launch (the
 // one-rank branch never merges its updates, so no row changes during the
 // iteration): one warp per work item, U neighbours in flight, split rows
-// combined in piece order.  Row i's update goes to Y[i] (FP32, from zero).
+// combined in piece order.  Row i's update goes to Y[i] (FP32, from zero).  The
+// launch is hundreds of thousands of warps, so resident warps hide the gather's
+// latency: at dim 128 the kernel is held to 48 registers for five CTAs per SM.
 template <int D, int U>
 __global__ void __launch_bounds__(kWarps * 32, D == 128 ? 5 : 1) sparse_attract_kernel(const SpmmArgs a) {
   const int lane = threadIdx.x & 31;
@@ -170,9 +172,10 @@ __device__ __forceinline__ uint64_t order_key(float v) {
 // shuffle, within a lane directly), after which sorted position p < dim - keep
 // names a dim to drop.  When half the row is dropped (density 0.5) the first
 // step of the last merge already puts the D/2 smallest pairs below position
-// D/2, and the remaining steps, which only order the halves, are skipped.  T = double: the FP64 rows (absent = INT_MIN) and their
-// mirror; T = float: the mirror alone.  With `present` set the rows are pruned
-// only when floor(present / n) > keep (sparse_embedding.hpp:172-181), decided
+// D/2, and the remaining steps, which only order the halves, are skipped.
+// T = double: the FP64 rows (absent = INT_MIN) and their mirror; T = float: the
+// mirror alone.  With `present` set the rows are pruned only when
+// floor(present / n) > keep (sparse_embedding.hpp:172-181), decided
 // here so that the host need not wait.
 template <int D, typename T>
 __global__ void __launch_bounds__(256) sparse_prune_kernel(T *xs, float *x32, int64_t n, int32_t keep,
