@@ -917,15 +917,15 @@ def run_sparse_form(args):
     # Algorithmic bytes of a step.  Per iteration the attractive pass reads every
     # CSR entry's column id and FP32 neighbour row, each row's own row and work
     # item, and writes its FP32 update; the collector pass reads the updates and
-    # reads and writes the FP64 collector.  Once per step: the FP64 rows copied in
-    # (read + write) and mirrored (read FP64, write FP32); after the first iteration
+    # reads and writes the FP64 collector.  Once per step: the FP64 rows read in
+    # once and written with their FP32 mirror; after the first iteration
     # the present entries are counted (read FP64) and the pruning reads FP64 and
     # writes the dim - k dropped entries in FP64 and FP32 (the rows do not change
     # after it, so the later checks cannot prune); the final pass reads FP64 and
     # writes the absent entries.
     row32, row64 = 4 * dim, 8 * dim
     per_iter = nnz * (4 + row32) + n * (row32 + 32 + row32) + n * row32 + 2 * B * row64
-    once = 2 * n * row64 + n * (row64 + row32) + n * row64 + n * row64 + n * (dim - keep) * 12 \
+    once = 2 * n * row64 + n * row32 + n * row64 + n * row64 + n * (dim - keep) * 12 \
         + n * row64 + n * (dim - keep) * 8
     alg = iters * per_iter + once
     peak, peak_kind = measured_peak()

@@ -194,6 +194,9 @@ cudaError_t launch_sparse_attract(int dim, const SpmmArgs &a, cudaStream_t s);
 cudaError_t launch_sparse_collect(const float *y, double *coll, int64_t n, int32_t batch, int32_t dim,
                                   cudaStream_t s);
 cudaError_t launch_sparse_mirror(const double *x64, float *x32, int64_t count, cudaStream_t s);
+// src / dst: device or mapped pinned host memory, 16-byte aligned; count even
+cudaError_t launch_sparse_load(const double *src, double *x64, float *x32, int64_t count, cudaStream_t s);
+cudaError_t launch_sparse_store(const double *src, double *dst, int64_t count, cudaStream_t s);
 cudaError_t launch_sparse_count(const double *x64, int64_t count, unsigned long long *present, cudaStream_t s);
 cudaError_t launch_sparse_prune_f64(int dim, double *x64, float *x32, int64_t n, int32_t keep,
                                     const unsigned long long *present, cudaStream_t s);

@@ -713,6 +713,19 @@ static void *mapped_host(const void *p) {
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// A pointer kernels can read: device memory as it is, pinned host memory through
+// its device alias; nullptr for pageable host memory.
+static const double *device_view(const double *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+  if (at.type == cudaMemoryTypeHost) return static_cast<const double *>(at.devicePointer);
+  return nullptr;
+}
+
 static int copy_embeddings_f64(de_handle *h, double *host, bool to_device, float *dev = nullptr) {
   if (!h || !host) return fail(h, DE_ERR_INVALID, "NULL argument");
   DE_CUDA(h, cudaSetDevice(h->device));
@@ -946,9 +959,15 @@ int de_sparse_set(de_handle *h, const double *x) {
   const size_t count = size_t(h->n) * h->dim;
   if (!h->d_sx) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_sx), count * sizeof(double)));
   if (!h->d_present) DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_present), sizeof(unsigned long long)));
-  // x is host or device memory (unified addressing tells which)
-  DE_CUDA(h, cudaMemcpyAsync(h->d_sx, x, count * sizeof(double), cudaMemcpyDefault, h->stream));
-  DE_CUDA(h, launch_sparse_mirror(h->d_sx, h->d_x, int64_t(count), h->stream));
+  // Device memory or pinned host memory: one kernel reads it once and writes
+  // the rows and their mirror; pageable host memory: a copy, then the mirror.
+  const double *src = device_view(x);
+  if (src && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    DE_CUDA(h, launch_sparse_load(src, h->d_sx, h->d_x, int64_t(count), h->stream));
+  } else {
+    DE_CUDA(h, cudaMemcpyAsync(h->d_sx, x, count * sizeof(double), cudaMemcpyDefault, h->stream));
+    DE_CUDA(h, launch_sparse_mirror(h->d_sx, h->d_x, int64_t(count), h->stream));
+  }
   h->sparse_in_mirror = false;
   return DE_OK;
 }
@@ -1034,7 +1053,14 @@ int de_sparse_get(de_handle *h, double *x, double *coll) {
     DE_CUDA(h, launch_f32_to_f64(h->d_x, h->d_sx, int64_t(count), h->stream));
     h->sparse_in_mirror = false;
   }
-  if (x) DE_CUDA(h, cudaMemcpyAsync(x, h->d_sx, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (x) {
+    // pinned host memory is written by a kernel over the host link
+    double *dst = static_cast<double *>(mapped_host(x));
+    if (dst && (reinterpret_cast<uintptr_t>(dst) & 15) == 0)
+      DE_CUDA(h, launch_sparse_store(h->d_sx, dst, int64_t(count), h->stream));
+    else
+      DE_CUDA(h, cudaMemcpyAsync(x, h->d_sx, count * sizeof(double), cudaMemcpyDefault, h->stream));
+  }
   if (coll) {
     if (!h->d_coll || h->sparse_batch <= 0) return fail(h, DE_ERR_INVALID, "no batch collector: run first");
     DE_CUDA(h, cudaMemcpyAsync(coll, h->d_coll, size_t(h->sparse_batch) * h->dim * sizeof(double),

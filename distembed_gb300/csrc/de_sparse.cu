@@ -134,6 +134,25 @@ __global__ void __launch_bounds__(256) sparse_mirror_kernel(const double *__rest
   }
 }
 
+// Rows in: x64 = src and its mirror x32 in one pass over src (device memory, or
+// pinned host memory read over the host link); two entries per thread step.
+__global__ void __launch_bounds__(256) sparse_load_kernel(const double2 *__restrict__ src, double2 *__restrict__ x64,
+                                                          float2 *__restrict__ x32, int64_t pairs) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < pairs; e += int64_t(gridDim.x) * blockDim.x) {
+    const double2 v = src[e];
+    x64[e] = v;
+    x32[e] = make_float2(__double_as_longlong(v.x) == int64_t(kAbsent64) ? 0.f : float(v.x),
+                         __double_as_longlong(v.y) == int64_t(kAbsent64) ? 0.f : float(v.y));
+  }
+}
+
+// Rows out: dst = src, two entries per thread step (dst: pinned host memory).
+__global__ void __launch_bounds__(256) sparse_store_kernel(const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                                           int64_t pairs) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < pairs; e += int64_t(gridDim.x) * blockDim.x)
+    dst[e] = src[e];
+}
+
 // Present entries (value != INT_MIN) of the FP64 rows, added to *present.
 __global__ void __launch_bounds__(256) sparse_count_kernel(const double *__restrict__ x64, int64_t count,
                                                            unsigned long long *present) {
@@ -285,6 +304,23 @@ cudaError_t launch_sparse_collect(const float *y, double *coll, int64_t n, int32
 cudaError_t launch_sparse_mirror(const double *x64, float *x32, int64_t count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   sparse_mirror_kernel<<<elementwise_grid(count), 256, 0, s>>>(x64, x32, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sparse_load(const double *src, double *x64, float *x32, int64_t count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  if ((count & 1) || (reinterpret_cast<uintptr_t>(src) & 15)) return cudaErrorInvalidValue;
+  sparse_load_kernel<<<elementwise_grid(count / 2), 256, 0, s>>>(
+      reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(x64), reinterpret_cast<float2 *>(x32),
+      count / 2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sparse_store(const double *src, double *dst, int64_t count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  if ((count & 1) || (reinterpret_cast<uintptr_t>(dst) & 15)) return cudaErrorInvalidValue;
+  sparse_store_kernel<<<elementwise_grid(count / 2), 256, 0, s>>>(reinterpret_cast<const double2 *>(src),
+                                                                  reinterpret_cast<double2 *>(dst), count / 2);
   return cudaGetLastError();
 }
 

@@ -119,3 +119,24 @@ def test_unsupported_handles_refuse():
     with de.Handle(rp, col, 64) as h:
         with pytest.raises(de.DEError):
             h.sparse_run(1, 256, 5, 0.05, 0.5)  # no rows uploaded
+
+
+@pytest.mark.parametrize("merge", [False, True])
+def test_pinned_and_device_rows_equal_pageable(merge):
+    # pinned host rows and device rows are read and written by kernels, pageable
+    # rows by copies: the same results either way
+    torch = pytest.importorskip("torch")
+    n, rp, col = graph("rmat", 51)
+    x = f32(gg.init_embedding(n, 64, seed=52))
+    x[::7, 3] = ABSENT
+    with de.Handle(rp, col, 64) as h:
+        want_x, want_c = h.sparse_embedding(x, 3, 200, 5, 0.05, 0.5, merge=merge)
+        pinned = torch.empty((n, 64), dtype=torch.float64, pin_memory=True).numpy()
+        pinned[:] = x
+        coll = torch.empty((200, 64), dtype=torch.float64, pin_memory=True).numpy()
+        h.sparse_embedding(pinned, 3, 200, 5, 0.05, 0.5, merge=merge, inplace=True, coll=coll)
+        h.sparse_set(torch.from_numpy(x).to("cuda"))
+        h.sparse_run(3, 200, 5, 0.05, 0.5, merge=merge)
+        dev_x, dev_c = h.sparse_get()
+    assert np.array_equal(pinned, want_x) and np.array_equal(coll, want_c)
+    assert np.array_equal(dev_x, want_x) and np.array_equal(dev_c, want_c)
