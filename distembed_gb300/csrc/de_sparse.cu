@@ -257,9 +257,16 @@ __global__ void __launch_bounds__(256) sparse_prune_kernel(T *xs, float *x32, in
 
 // After the last iteration absent entries become 0 (the final CSR build with
 // clear_dense_collector, cpp/core/distributed_mat.hpp:63-91).
-__global__ void __launch_bounds__(256) sparse_finalize_kernel(double *__restrict__ x64, int64_t count) {
-  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < count; e += int64_t(gridDim.x) * blockDim.x)
-    if (__double_as_longlong(x64[e]) == int64_t(kAbsent64)) x64[e] = 0.0;
+// Two entries per thread step; a pair is written back only when it held one.
+__global__ void __launch_bounds__(256) sparse_finalize_kernel(double2 *__restrict__ x64, int64_t pairs) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < pairs; e += int64_t(gridDim.x) * blockDim.x) {
+    double2 v = x64[e];
+    const bool ax = __double_as_longlong(v.x) == int64_t(kAbsent64);
+    const bool ay = __double_as_longlong(v.y) == int64_t(kAbsent64);
+    if (ax) v.x = 0.0;
+    if (ay) v.y = 0.0;
+    if (ax || ay) x64[e] = v;
+  }
 }
 
 template <typename T>
@@ -341,7 +348,8 @@ cudaError_t launch_sparse_prune_f32(int dim, float *x32, int64_t n, int32_t keep
 
 cudaError_t launch_sparse_finalize(double *x64, int64_t count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  sparse_finalize_kernel<<<elementwise_grid(count), 256, 0, s>>>(x64, count);
+  if (count & 1) return cudaErrorInvalidValue;  // n x dim with dim a multiple of 32
+  sparse_finalize_kernel<<<elementwise_grid(count / 2), 256, 0, s>>>(reinterpret_cast<double2 *>(x64), count / 2);
   return cudaGetLastError();
 }
 
