@@ -153,3 +153,20 @@ def test_reader_reports_the_first_bad_entry_by_number(tmp_path):
         f.write("%%MatrixMarket matrix coordinate pattern general\n3 3 4\n1 2\n2 3\n")
     with pytest.raises(de.DEError, match="ends early"):
         de.read_mtx(t)
+
+
+def test_transpose_csr_is_the_receiver_matrix():
+    # the CSR the reference's col_major flag selects: entries (j, i) for every (i, j),
+    # columns ascending in each row; transposing twice gives the input back
+    from distembed_gb300 import graphgen as gg
+    rng = np.random.default_rng(61)
+    n = 300
+    src, dst = rng.integers(0, n, 2000), rng.integers(0, n, 2000)
+    rp, col = gg.coo_to_csr(n, src, dst)
+    trp, tcol = gg.transpose_csr(rp, col)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    trows = np.repeat(np.arange(n), np.diff(trp))
+    assert set(zip(rows.tolist(), col.tolist())) == set(zip(tcol.tolist(), trows.tolist()))
+    assert all(np.all(np.diff(tcol[trp[i]:trp[i + 1]]) > 0) for i in range(n))
+    back = gg.transpose_csr(trp, tcol)
+    assert np.array_equal(back[0], rp) and np.array_equal(back[1], col)
