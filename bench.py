@@ -1,26 +1,42 @@
 #!/usr/bin/env python
 """Benchmark of the force-model SGD embedding step on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form F]
 
-Workload (the FP32 plain GPU path at scale): R-MAT scale 20 (1,048,576 vertices,
-edge factor 16, a=.57 b=.19 c=.19, seed 1, symmetrised, duplicates and self-loops
-removed), dim 128, minibatch 4096, 5 shared negatives per minibatch, lr 0.02,
-a 10-epoch job; embedding initialised U[-0.5, 0.5] (seed 0).  Synthetic data.
+Default line (the metric: edge-updates/s of the BF16 batched form against the
+FP32 plain form on one GB300, final loss against the FP64 oracle, job p50/p99):
 
-A step is one epoch of that job (256 minibatches); step k runs epoch k mod 10
-with the reference's seeds.  `value` = edge-updates/s with the graph and the
-embedding resident in HBM; `e2e` = the same metric through the reference-facing
-call (host FP64 embedding in, 10 epochs, host FP64 embedding out) with the
-host<->device copies inside the timed region.  The embedding (512 MiB) is larger
-than L2, so no flush is needed between steps.
+  workload  512 independent graphs, vertex counts log-uniform in [500, 50,000]
+            (seed 3); even positions kNN graphs (k=10 of 32-D 10-component Gaussian
+            mixtures), odd positions R-MAT (edge factor 8); dim 64, minibatch 256,
+            5 shared negatives per minibatch, lr 0.02, 20 epochs per graph,
+            U[-0.5, 0.5] initial embeddings (seed 1000 + graph).  Synthetic data.
+  step      one persistent launch (a CUDA graph) that trains every graph for its
+            20 epochs with BF16 storage, FP32 master copy and FP32 arithmetic; the
+            embeddings are reset to their start values before every step (untimed).
+  value     edge-updates/s (attractive CSR entries plus repulsive (row, valid
+            negative) pairs, counted exactly) with everything resident in HBM.
+  e2e       the same job through the public call with the host FP32 embeddings
+            copied in and out (pinned), the host sampler and graph capture inside.
+  compare   the same 512 graphs with FP32 storage in the same launch; the FP32 plain
+            form graph by graph; the FP32 plain form on its own workload (R-MAT
+            scale 20, ef 16, dim 128, minibatch 4096, 10-epoch job).
+  loss      every graph's final-epoch loss against the FP64 oracle (the reference's
+            algorithm in FP64) run on the same graph.
+  served    the served form on a Poisson stream (200 jobs/s, the configuration's
+            rate) and at half the measured capacity: p50/p99 job latency.
+  cpu_baseline  the FP64 port (-O3) on every host core, one graph per thread.
 
---impl reference times the reference's CPU algorithm (the FP64 oracle port in
-oracle/, OpenMP over all host cores, same loop structure as cpp/algo/algo.hpp)
-on the same workload; each step is one minibatch of the epoch.
+--impl reference times the reference's CPU algorithm (the FP64 port in oracle/,
+-O3, every host core, one graph per thread) on the same 512 graphs; one step is
+one epoch of every graph.  --form plain|bf16|batched|served|spmm|sparse prints the
+line of one form alone (plain: R-MAT scale 20; bf16: R-MAT scale 22, dim 256, 1024
+shared negatives; batched: the default workload without the other forms; served:
+the arrival stream; spmm and sparse: the "next" steps on R-MAT scale 20).
 
 For N > 1 (torchrun) every rank runs an independent replica on its own GPU
-(the path does not shard: one resident partition); value sums over ranks.
+(the path does not shard: each job is one resident partition); value sums over
+ranks, time is the slowest rank's.
 """
 from __future__ import annotations
 
@@ -48,23 +64,27 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=300)
-    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--pdl", type=int, default=1, help="overlap consecutive minibatch launches")
-    p.add_argument("--edge-cap", type=int, default=0, help="max CSR entries per work item (0: automatic)")
-    p.add_argument("--form", default="plain", choices=["plain", "bf16", "batched", "served", "spmm", "sparse"],
-                   help="plain: FP32 plain form on R-MAT s20 (default line); bf16: BF16 precision form vs the "
-                        "FP32 plain form on R-MAT s22, dim 256, 1024 shared negatives; batched: 512 graphs in one "
-                        "persistent launch, BF16 storage, vs the FP32 plain form on the same graphs")
-    p.add_argument("--graphs", type=int, default=512, help="batched form: number of graphs")
+    p.add_argument("--pdl", type=int, default=1, help="plain form: overlap consecutive minibatch launches")
+    p.add_argument("--edge-cap", type=int, default=0, help="plain form: max CSR entries per work item (0: automatic)")
+    p.add_argument("--form", default="headline",
+                   choices=["headline", "plain", "bf16", "batched", "served", "spmm", "sparse"],
+                   help="headline (default): the metric's comparison on the batched workload with every other "
+                        "form beside it; the others print one form alone")
+    p.add_argument("--graphs", type=int, default=512, help="batched workload: number of graphs")
     p.add_argument("--jobs", type=int, default=256, help="served form: jobs in the arrival stream")
     p.add_argument("--scale", type=int, default=0, help="bf16 form: R-MAT scale instead of 22 (small profiling cases)")
     p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
+    p.add_argument("--served-precision", default="bf16", choices=["bf16", "fp32"],
+                   help="served form: storage of the jobs (dim 32 jobs run FP32: the BF16 form takes 64-256)")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
+    p.add_argument("--no-served", action="store_true", help="headline: skip the served legs")
+    p.add_argument("--no-gap", action="store_true", help="skip the FP64 oracle runs (loss gaps)")
     p.add_argument("--shape", default="", help="batched form: team shape instead of the autotuner, "
                                                "staged|rows:W:cap:steps:stages[:ctas] or register:vpw:W:cap")
     return p.parse_args()
@@ -112,9 +132,10 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "plain_batch_kernel_rmat20.txt")
+def profile_traffic(name="plain_batch_kernel_rmat20.txt"):
+    """DRAM bytes per launch of a kernel from its committed ncu summary (the line
+    `dram_bytes_per_launch_scaled: <bytes>`), or None."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch_scaled:"):
@@ -168,8 +189,9 @@ class Clocks:
 
 
 def cpu_sample(rowptr, col, x0, seconds):
-    """The FP64 oracle (the reference's algorithm, its OpenMP structure) on host
-    cores: stride-sampled minibatches of epoch 0 until `seconds` have passed."""
+    """The FP64 port (the reference's algorithm and its OpenMP structure, -O3
+    build, no loss) on every host core: stride-sampled minibatches of epoch 0
+    until `seconds` have passed."""
     import oracle
     n = len(rowptr) - 1
     batches = (n + W["batch"] - 1) // W["batch"]
@@ -179,57 +201,23 @@ def cpu_sample(rowptr, col, x0, seconds):
     updates, done, t0 = 0, 0, time.perf_counter()
     for j in order:
         updates += oracle.run_batches(rowptr, col, x, 0, W["batch"], W["ns"], W["lr"], [j], quirks=True,
-                                      threads=threads)
+                                      threads=threads, fast=True)
         done += 1
         if time.perf_counter() - t0 >= seconds:
             break
     dt = time.perf_counter() - t0
     return {"value": updates / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "build": "g++ -O3 -ffp-contract=fast -fopenmp (oracle/liboracle_fast.so)",
             "sample": f"{done} of {batches} minibatches of epoch 0 (stride-8 order), FP64, {updates} edge-updates "
-                      f"in {dt:.1f} s"}
+                      f"in {dt:.1f} s, OpenMP over the rows of a minibatch as the reference"}
 
-
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    import oracle
-    n, rowptr, col, x0 = workload()
-    batches = (n + W["batch"] - 1) // W["batch"]
-    x = np.array(x0, dtype=np.float64, copy=True)
-    threads = os.cpu_count() or 1
-
-    def step(k):
-        j = (37 * k) % batches
-        return oracle.run_batches(rowptr, col, x, 0, W["batch"], W["ns"], W["lr"], [j], quirks=True, threads=threads)
-
-    for k in range(args.warmup):
-        step(k)
-    t0 = time.perf_counter()
-    updates = sum(step(args.warmup + k) for k in range(args.steps))
-    dt = time.perf_counter() - t0
-    v = updates / dt
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)),
-                                            "step": "one minibatch of epoch 0 (j = 37k mod 256)",
-                                            "parallelism": "1 process x all host cores (OpenMP)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} minibatches, FP64, {updates} edge-updates"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def run_ours(args):
+def plain_leg(args, rank, world, local, with_cpu, with_gap):
+    """The FP32 plain form on R-MAT scale 20 (dim 128, minibatch 4096, 10-epoch
+    job): one step = one epoch.  Returns the line of this form (the keys of the
+    bench contract) or None on ranks other than 0."""
     import torch
 
     import distembed_gb300 as de
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as tdist
-        tdist.init_process_group("gloo")
-    torch.cuda.set_device(local)
     n, rowptr, col, x0 = workload()
     dim, B, ns, lr, E = W["dim"], W["batch"], W["ns"], W["lr"], W["epochs"]
     batches = (n + B - 1) // B
@@ -277,6 +265,7 @@ def run_ours(args):
     serial_achieved = alg_epoch / (float(pms[kind == 0].sum()) / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = profile_traffic()
+    dram_gbs = traffic * batches / mean_epoch_s / 1e9 if traffic else None
 
     # end to end: the reference-facing call on pinned host FP64 buffers
     e2e = None
@@ -302,34 +291,66 @@ def run_ours(args):
                "step": "EmbeddingAlgo call: host FP64 x in, 10 epochs, host FP64 x out (pinned)",
                "ms_per_step": 1e3 * e2e_s, "final_loss": float(loss[-1])}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_sample(rowptr, col, x0, args.cpu_seconds)
+    gap = None
+    if rank == 0 and world == 1 and with_gap:
+        # the whole 10-epoch job against the FP64 oracle at full size, from the
+        # same (FP32-rounded) start
+        import oracle
+        xs = x0.astype(np.float32).astype(np.float64)
+        h.set_embeddings(xs)
+        gloss = h.run(E, B, ns, lr, want_loss=True)
+        gx = h.get_embeddings()
+        t1 = time.perf_counter()
+        ox, oloss = oracle.run(rowptr, col, xs, E, B, ns, lr, quirks=True, threads=os.cpu_count() or 1)
+        gap = {"loss_rel_per_epoch": [float(v) for v in np.abs(gloss - oloss) / oloss],
+               "loss_rel_max": float(np.max(np.abs(gloss - oloss) / oloss)),
+               "final_loss_rel": float(abs(gloss[-1] - oloss[-1]) / oloss[-1]),
+               "x_rel_l2": float(np.linalg.norm(gx - ox) / np.linalg.norm(ox)),
+               "oracle_s": round(time.perf_counter() - t1, 1),
+               "bound": "per-epoch loss within 1e-3, embedding within 1e-4 relative L2 (tests/test_gpu_cfg2.py)"}
 
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: R-MAT scale 20 (ef 16, a.57 b.19 c.19, seed 1), U[-0.5,0.5] init (seed 0)",
-            "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)), "dim": dim, "batch": B, "ns": ns,
-                       "lr": lr, "epochs_per_job": E, "step": "one epoch (256 minibatches, CUDA graph)",
-                       "l2": "inputs larger than L2 (512 MiB FP32 embedding); no flush",
-                       "parallelism": "replicas" if world > 1 else "single GPU", "ref_quirks": True,
-                       "pdl": bool(args.pdl), "edge_cap": args.edge_cap},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                         "kernel": "plain_batch_kernel<128>",
-                         "algorithmic_bytes_per_epoch": alg_epoch,
-                         "note": "achieved = algorithmic bytes / epoch time over 256 launches (gaps included)",
-                         "launch_us_serial": launch_us, "achieved_serial_launches": serial_achieved},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "gpu_launches": args.steps * (batches + 1),
-            "clocks": clk,
-        }
-        print(json.dumps(line), flush=True)
+    cpu = None
+    if rank == 0 and world == 1 and with_cpu:
+        cpu = cpu_sample(rowptr, col, x0, args.cpu_seconds)
     h.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: R-MAT scale 20 (ef 16, a.57 b.19 c.19, seed 1), U[-0.5,0.5] init (seed 0)",
+        "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)), "dim": dim, "batch": B, "ns": ns,
+                   "lr": lr, "epochs_per_job": E, "step": "one epoch (256 minibatches, CUDA graph)",
+                   "l2": "inputs larger than L2 (512 MiB FP32 embedding); no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "ref_quirks": True,
+                   "pdl": bool(args.pdl), "edge_cap": args.edge_cap},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "kernel": "plain_batch_kernel<128>",
+                     "algorithmic_bytes_per_epoch": alg_epoch,
+                     "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak if dram_gbs else None,
+                     "note": "achieved = algorithmic bytes / epoch time over 256 launches (gaps included); "
+                             "dram_gbs = ncu DRAM bytes per launch (profiles/plain_batch_kernel_rmat20.txt) x "
+                             "launches / epoch time",
+                     "launch_us_serial": launch_us, "achieved_serial_launches": serial_achieved},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gap_vs_fp64_oracle": gap,
+        "gpu_launches": args.steps * (batches + 1),
+        "clocks": clk,
+    }
+
+
+def run_plain_form(args):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    line = plain_leg(args, rank, world, local, with_cpu=not args.no_cpu_baseline, with_gap=not args.no_gap)
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -449,7 +470,6 @@ def run_bf16_form(args):
                         "final_loss_gap_vs_fp32": gap}}
     print(json.dumps(line), flush=True)
 
-
 W4 = dict(n_lo=500, n_hi=50000, seed=3, dim=64, batch=256, ns=5, lr=0.02, epochs=20, init_seed=1000,
           knn_k=10, knn_dim=32, rmat_ef=8)
 
@@ -463,188 +483,245 @@ def batched_workload(count, device):
     return graphs, x0
 
 
+def batched_config(graphs):
+    """The workload of the default line (the same dict in both arms)."""
+    return {"workload": f"batched{len(graphs)}_knn_rmat_d64_b256_ns5_e20", "graphs": len(graphs),
+            "vertices": int(sum(n for _, n, _, _ in graphs)), "nnz": int(sum(len(c) for _, _, _, c in graphs)),
+            "dim": W4["dim"], "batch": W4["batch"], "ns": W4["ns"], "lr": W4["lr"], "epochs_per_job": W4["epochs"],
+            "kinds": "even graphs kNN (k=10, 32-D 10-component mixtures), odd graphs R-MAT (ef 8)",
+            "ref_quirks": True}
+
+
+BATCHED_DATA = ("synthetic: {g} graphs, n log-uniform [500, 50000] (seed 3), even: kNN k=10 of 32-D 10-component "
+                "mixtures (FP32 kNN on the GPU), odd: R-MAT ef 8; U[-0.5,0.5] init (seed 1000+i)")
+
+
 def batched_bytes_per_epoch(graphs, dim, B, ns, s=2):
     """Algorithmic bytes of one epoch of every graph (no reuse credited): per CSR
-    entry its column id and the BF16 neighbour row; per vertex its rowptr entry,
-    its own BF16 row read, the FP32 master read and written and the BF16 copy
-    written; per minibatch the ns negative rows."""
+    entry its column id and the neighbour row (s bytes per component); per vertex
+    its rowptr entry, its own row read, the FP32 master read and written and (BF16)
+    the BF16 copy written; per minibatch the ns negative rows."""
     tot = 0
     for _, n, rp, c in graphs:
         nnz_eff = len(c) - int(np.sum(c == n - 1))
         batches = (n + B - 1) // B
-        tot += nnz_eff * (4 + dim * s) + n * (8 + dim * s + 2 * dim * 4 + dim * s) + batches * ns * dim * s
+        copy = dim * s if s == 2 else 0
+        tot += nnz_eff * (4 + dim * s) + n * (8 + dim * s + 2 * dim * 4 + copy) + batches * ns * dim * s
     return tot
 
 
-def run_batched_form(args):
-    """Batched form: every graph of the suite trained for 20 epochs in one persistent
-    launch (BF16 storage, FP32 master), against the FP32 plain form on the same
-    graphs one after the other."""
+def parse_shape(text):
+    f = text.split(":")
+    if f[0] in ("staged", "rows"):
+        return dict(kernel=f[0], team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]),
+                    team_ctas=int(f[5]) if len(f) > 5 else 1)
+    return dict(kernel="register", vertices_per_warp=int(f[1]), team_warps=int(f[2]), edge_cap=int(f[3]))
+
+
+def batched_leg(graphs, x0_all, precision, local, steps, warmup, e2e_steps=0, shape=None, clocks=False):
+    """The batched form on `graphs`: autotuned (or the given shape), then `warmup`
+    untimed and `steps` timed launches of the whole 20-epoch job, the embeddings
+    reset to x0_all before each (untimed).  Returns a dict of measurements."""
     import torch
 
     import distembed_gb300 as de
-    import oracle
-    torch.cuda.set_device(0)
-    t0 = time.perf_counter()
-    graphs, x0 = batched_workload(args.graphs, "cuda")
-    gen_s = time.perf_counter() - t0
     dim, B, ns, lr, E = W4["dim"], W4["batch"], W4["ns"], W4["lr"], W4["epochs"]
     total_n = int(sum(n for _, n, _, _ in graphs))
-    total_nnz = int(sum(len(c) for _, _, _, c in graphs))
-    x0_all = np.concatenate(x0)
-
-    b = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="bf16")
-    stream = torch.cuda.ExternalStream(b.stream, device=0)
-    b.set_embeddings(-1, x0_all)
+    b = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision=precision, device=local)
+    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    x_start = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+    x_start[:] = x0_all
+    b.set_embeddings(-1, x_start)
     t0 = time.perf_counter()
-    if args.shape:
-        f = args.shape.split(":")
-        if f[0] in ("staged", "rows"):
-            b.set_shape(kernel=f[0], team_warps=int(f[1]), edge_cap=int(f[2]), pairs=int(f[3]), stages=int(f[4]),
-                        team_ctas=int(f[5]) if len(f) > 5 else 1)
-        else:
-            b.set_shape(kernel="register", vertices_per_warp=int(f[1]), team_warps=int(f[2]), edge_cap=int(f[3]))
-        shape, tuned = b.shape(), []
-    else:
+    tuned = []
+    if shape:
+        try:
+            b.set_shape(**shape)
+            b.prepare(E, B, ns, lr)
+        except de.DEError:  # the shape does not fit this precision: tune
+            shape = None
+    if not shape:
         shape, tuned = b.autotune(1, B, ns, lr)
     tune_s = time.perf_counter() - t0
     upd = b.edge_updates(E, B, ns)
     b.prepare(E, B, ns, lr)
-    # the job's own loss: one launch from the initial embedding
-    b.set_embeddings(-1, x0_all)
+    b.set_embeddings(-1, x_start)
     b.launch()
-    loss_bf16 = b.wait()
-    # every step is the same job: embeddings back to the start values (untimed),
-    # then the one launch (timed with events on the batch's stream)
-    x_start = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
-    x_start[:] = x0_all
-    for _ in range(args.warmup):
+    loss = b.wait()
+    trace = b.trace()
+    for _ in range(warmup):
         b.set_embeddings(-1, x_start)
         b.launch()
         b.wait()
-    clocks = Clocks(0)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    clk_rec = Clocks(local) if clocks else None
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
     torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
-    for k in range(args.steps):
+    if clk_rec:
+        clk_rec.start()
+        time.sleep(0.3)
+    for k in range(steps):
         b.set_embeddings(-1, x_start)
         ev[2 * k].record(stream)
         b.launch()
         ev[2 * k + 1].record(stream)
         b.wait()
     torch.cuda.synchronize()
-    clk = clocks.stop()
-    step_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
-    total_s = sum(step_ms) / 1e3
-    value = upd * args.steps / total_s
-
-    # end to end through the public API: pinned host FP32 in, the job, host out
-    x_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
-    x_host[:] = x0_all
-    out_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
-    e2e_t = []
-    for k in range(max(args.e2e_steps, 0) + 1):
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        b.set_embeddings(-1, x_host)
-        b.launch()
-        b.wait()
-        b.get_embeddings(-1, out=out_host)
-        if k > 0:
-            e2e_t.append(time.perf_counter() - t1)
+    clk = clk_rec.stop() if clk_rec else None
+    step_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(steps)]
     e2e = None
-    if e2e_t:
-        e2e_s = statistics.mean(e2e_t)
-        e2e = {"value": upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": total_n * dim * 4,
-               "d2h_bytes_per_step": total_n * dim * 4, "ms_per_step": 1e3 * e2e_s,
-               "step": "host FP32 embeddings of every graph in, the 20-epoch job, host FP32 out (pinned)"}
+    if e2e_steps > 0:
+        # the public call: host FP32 embeddings in, de_batch_run (host sampler,
+        # upload of the draws, graph capture, the launch, the losses back), host out
+        x_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+        x_host[:] = x0_all
+        out_host = torch.empty((total_n, dim), dtype=torch.float32, pin_memory=True).numpy()
+        ts = []
+        for k in range(e2e_steps + 1):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            b.set_embeddings(-1, x_host)
+            b.run(E, B, ns, lr)
+            b.get_embeddings(-1, out=out_host)
+            if k > 0:
+                ts.append(time.perf_counter() - t1)
+        negs = sum(((n + B - 1) // B) * E * ns for _, n, _, _ in graphs)
+        e2e = {"value": upd / statistics.mean(ts), "unit": UNIT,
+               "h2d_bytes_per_step": total_n * dim * 4 + negs * 4 + E * 4,
+               "d2h_bytes_per_step": total_n * dim * 4 + len(graphs) * E * 8,
+               "ms_per_step": 1e3 * statistics.mean(ts),
+               "step": "host FP32 embeddings of every graph in (pinned), de_batch_run (host sampler, draws "
+                       "uploaded, graph captured, the 20-epoch launch, losses back), host FP32 out"}
+        b.prepare(E, B, ns, lr)
     b.close()
+    span = trace[:, 1] - trace[:, 0]
+    return {"edge_updates": upd, "step_ms": step_ms, "value": upd / (sum(step_ms) / 1e3), "loss": loss,
+            "shape": shape, "tuned": tuned, "tune_s": tune_s, "e2e": e2e, "clocks": clk,
+            "trace": {"makespan_ms": float(trace[:, 1].max()) / 1e6, "longest_graph_ms": float(span.max()) / 1e6,
+                      "graph_ms_sum": float(span.sum()) / 1e6, "teams": int(len(np.unique(trace[:, 2])))}}
 
-    # FP32 storage in the same batched launch: the loss the BF16 storage is held to
-    bf = de.Batch([(rp, c) for _, _, rp, c in graphs], dim, precision="fp32")
-    try:
-        bf.set_shape(**shape)
-        bf.prepare(E, B, ns, lr)
-    except de.DEError:  # the shape's FP32 rows do not fit in shared memory: the autotuner picks one
-        bf.autotune(1, B, ns, lr)
-    bf.set_embeddings(-1, x0_all)
-    loss_fp32 = bf.run(E, B, ns, lr)
-    bf.close()
-    gap_fp32 = np.abs(loss_bf16[:, -1] - loss_fp32[:, -1]) / loss_fp32[:, -1]
 
-    # FP64 oracle on a sample of graphs (the 8 smallest), full job
-    order = np.argsort([n for _, n, _, _ in graphs])[:8]
-    gaps = []
-    for i in order:
-        _, n, rp, c = graphs[i]
-        _, lo = oracle.run(rp, c, x0[i].astype(np.float64), E, B, ns, lr, quirks=True, threads=os.cpu_count() or 1)
-        gaps.append(abs(loss_bf16[i, -1] - lo[-1]) / lo[-1])
+def plain_same_graphs(graphs, x0, local):
+    """The FP32 plain form on the same graphs, one graph after another: device
+    time of each 20-epoch job summed (the graph capture of each job untimed)."""
+    import torch
 
-    # FP32 plain form on the same graphs, one graph after another
-    plain = None
-    if not args.no_plain_compare:
-        plain_ms, plain_upd = 0.0, 0
-        for i, (_, n, rp, c) in enumerate(graphs):
-            with de.Handle(rp, c, dim, quirks=True, compute_loss=True) as h:
-                st = torch.cuda.ExternalStream(h.stream, device=0)
-                h.set_embeddings(x0[i])
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                h.run(1, B, ns, lr, want_loss=False)            # capture outside the timed region
-                h.set_embeddings(x0[i])
-                h.sync()
-                e0.record(st)
-                h.run(E, B, ns, lr, want_loss=False)
-                e1.record(st)
-                h.sync()
-                plain_ms += e0.elapsed_time(e1)
-                plain_upd += h.edge_updates(E, B, ns)
-        plain = {"edge_updates_per_s": plain_upd / (plain_ms / 1e3), "job_ms": plain_ms,
-                 "note": "FP32 plain form, one graph after another, device time of each 20-epoch job summed"}
+    import distembed_gb300 as de
+    B, ns, lr, E, dim = W4["batch"], W4["ns"], W4["lr"], W4["epochs"], W4["dim"]
+    plain_ms, plain_upd = 0.0, 0
+    for i, (_, n, rp, c) in enumerate(graphs):
+        with de.Handle(rp, c, dim, quirks=True, compute_loss=True, device=local) as h:
+            st = torch.cuda.ExternalStream(h.stream, device=local)
+            h.set_embeddings(x0[i])
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            h.run(1, B, ns, lr, want_loss=False)            # capture outside the timed region
+            h.set_embeddings(x0[i])
+            h.sync()
+            e0.record(st)
+            h.run(E, B, ns, lr, want_loss=False)
+            e1.record(st)
+            h.sync()
+            plain_ms += e0.elapsed_time(e1)
+            plain_upd += h.edge_updates(E, B, ns)
+    return {"edge_updates_per_s": plain_upd / (plain_ms / 1e3), "job_ms": plain_ms,
+            "note": "FP32 plain form, one graph after another, device time of each 20-epoch job summed"}
 
-    alg = batched_bytes_per_epoch(graphs, dim, B, ns) * E
+
+def gap_stats(loss, ref, kinds):
+    """Per-graph final-epoch relative gaps of `loss` against `ref` ([graphs, epochs])."""
+    g = np.abs(loss[:, -1] - ref[:, -1]) / ref[:, -1]
+
+    def st(sel):
+        v = g[sel]
+        return {"graphs": int(len(v)), "p50": float(np.percentile(v, 50)), "p90": float(np.percentile(v, 90)),
+                "max": float(v.max()), "within_1pct": int(np.sum(v <= 0.01))}
+
+    kinds = np.asarray(kinds)
+    job = np.abs(loss.sum(0) - ref.sum(0)) / ref.sum(0)
+    return {"job_sum_final": float(job[-1]), "job_sum_max_over_epochs": float(job.max()),
+            "all": st(np.ones(len(g), bool)), "knn": st(kinds == "knn"), "rmat": st(kinds == "rmat")}
+
+
+def fp64_oracle_losses(graphs, x0):
+    """Every graph's 20-epoch job in the FP64 oracle (bit-exact build, one graph
+    per host thread): loss [graphs, epochs]."""
+    import oracle
+    xs = [np.ascontiguousarray(x, dtype=np.float64) for x in x0]
+    _, loss = oracle.run_many([(rp, c) for _, _, rp, c in graphs], xs, W4["epochs"], W4["batch"], W4["ns"],
+                              W4["lr"], threads=os.cpu_count() or 1)
+    return loss
+
+
+def batched_cpu_baseline(graphs, x0, seconds):
+    """The FP64 port (-O3 build, no loss) on every host core, one graph per
+    thread: whole epochs of every graph until `seconds` have passed."""
+    import oracle
+    xs = [np.ascontiguousarray(x, dtype=np.float64) for x in x0]
+    threads = os.cpu_count() or 1
+    csr = [(rp, c) for _, _, rp, c in graphs]
+    u, e, t0 = 0, 0, time.perf_counter()
+    while e < W4["epochs"]:
+        du, _ = oracle.run_many(csr, xs, 1, W4["batch"], W4["ns"], W4["lr"], first_epoch=e, want_loss=False,
+                                threads=threads, fast=True)
+        u += du
+        e += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": u / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "build": "g++ -O3 -ffp-contract=fast -fopenmp (oracle/liboracle_fast.so)",
+            "sample": f"epochs 0..{e - 1} of all {len(graphs)} graphs, FP64, one graph per thread, {u} edge-updates "
+                      f"in {dt:.1f} s"}
+
+
+def roofline_batched(graphs, step_ms, precision="bf16"):
+    alg = batched_bytes_per_epoch(graphs, W4["dim"], W4["batch"], W4["ns"], s=2 if precision == "bf16" else 4) \
+        * W4["epochs"]
     mean_s = statistics.mean(step_ms) / 1e3
     peak, peak_kind = measured_peak()
+    traffic = profile_traffic("batched_kernel_batched512.txt")
     achieved = alg / mean_s / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "traffic": traffic, "kernel": "staged_kernel (batched, persistent)",
+            "algorithmic_bytes_per_launch": alg,
+            "dram_gbs": traffic / mean_s / 1e9 if traffic else None,
+            "dram_frac": traffic / mean_s / 1e9 / peak if traffic else None,
+            "note": "one launch per step; achieved = algorithmic bytes (no reuse credited) / launch time"}
 
-    # CPU baseline: the FP64 oracle, all host cores, whole jobs of graphs in suite order
-    cpu = None
-    if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        done, t1 = 0, time.perf_counter()
-        for i, (_, n, rp, c) in enumerate(graphs):
-            oracle.run(rp, c, x0[i].astype(np.float64), 1, B, ns, lr, quirks=True, threads=threads)
-            done += 1
-            if time.perf_counter() - t1 >= args.cpu_seconds:
-                break
-        dt = time.perf_counter() - t1
-        with de.Batch([(rp, c) for _, _, rp, c in graphs[:done]], dim) as bc:
-            cu = bc.edge_updates(1, B, ns)
-        cpu = {"value": cu / dt, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"epoch 0 of graphs 0..{done - 1} of the suite, FP64, {cu} edge-updates in {dt:.1f} s"}
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
-            "data": f"synthetic: {len(graphs)} graphs, n log-uniform [500, 50000] (seed 3), even: kNN k=10 of 32-D "
-                    "10-component mixtures, odd: R-MAT ef 8; U[-0.5,0.5] init (seed 1000+i)",
-            "config": {"workload": f"batched{len(graphs)}_d64_b256_ns5_e20_bf16", "graphs": len(graphs),
-                       "reset": "embeddings reset to the start values before every step (untimed)",
-                       "vertices": total_n, "nnz": total_nnz, "dim": dim, "batch": B, "ns": ns, "lr": lr,
-                       "epochs_per_job": E, "step": "one launch: every graph, 20 epochs (CUDA graph)",
-                       "l2": f"inputs larger than L2 ({total_n * dim * 6 / 2**30:.2f} GiB of embeddings); no flush",
-                       "team_shape": shape, "autotune_s": round(tune_s, 2), "autotune_shapes": len(tuned),
-                       "autotune_top5_ms": [[sh, round(t, 2)] for sh, t in sorted(tuned, key=lambda x: x[1])[:5]],
-                       "generate_s": round(gen_s, 1)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": None, "kernel": "batched_kernel",
-                         "algorithmic_bytes_per_launch": alg},
-            "loss": {"final_gap_vs_fp32_storage_max": float(gap_fp32.max()),
-                     "final_gap_vs_fp32_storage_mean": float(gap_fp32.mean()),
-                     "final_gap_vs_fp64_oracle_sample_max": float(max(gaps)), "oracle_sample_graphs": len(gaps)},
-            "compare": {"fp32_plain": plain,
-                        "batched_over_plain": (value / plain["edge_updates_per_s"]) if plain else None},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk}
+def run_batched_form(args):
+    """The batched form alone: BF16 batched against FP32 storage in the same launch,
+    the FP32 plain form on the same graphs, and the FP64 oracle on every graph."""
+    import torch
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    graphs, x0 = batched_workload(args.graphs, "cuda")
+    gen_s = time.perf_counter() - t0
+    x0_all = np.concatenate(x0)
+    kinds = [k for k, _, _, _ in graphs]
+    shape = parse_shape(args.shape) if args.shape else None
+    bf = batched_leg(graphs, x0_all, "bf16", 0, args.steps, args.warmup, args.e2e_steps, shape=shape, clocks=True)
+    f32 = batched_leg(graphs, x0_all, "fp32", 0, max(1, args.steps // 4), 1, 0, shape=bf["shape"])
+    plain = None if args.no_plain_compare else plain_same_graphs(graphs, x0, 0)
+    loss = None
+    if not args.no_gap:
+        lo = fp64_oracle_losses(graphs, x0)
+        loss = {"bf16_vs_fp64_oracle": gap_stats(bf["loss"], lo, kinds),
+                "fp32_storage_vs_fp64_oracle": gap_stats(f32["loss"], lo, kinds)}
+    cpu = None if args.no_cpu_baseline else batched_cpu_baseline(graphs, x0, args.cpu_seconds)
+    line = {"metric": METRIC, "value": bf["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.mean(bf["step_ms"]), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": BATCHED_DATA.format(g=len(graphs)),
+            "config": batched_config(graphs),
+            "impl_detail": {"team_shape": bf["shape"], "autotune_s": round(bf["tune_s"], 2),
+                            "autotune_shapes": len(bf["tuned"]), "trace": bf["trace"], "generate_s": round(gen_s, 1),
+                            "reset": "embeddings reset to the start values before every step (untimed)",
+                            "l2": "inputs larger than L2 (embeddings of every graph); no flush"},
+            "roofline": roofline_batched(graphs, bf["step_ms"]),
+            "loss": loss,
+            "compare": {"fp32_storage_batched": {"edge_updates_per_s": f32["value"],
+                                                 "ms_per_step": statistics.mean(f32["step_ms"]), "shape": f32["shape"]},
+                        "fp32_plain_same_graphs": plain},
+            "cpu_baseline": cpu, "e2e": bf["e2e"], "gpu_launches": args.steps, "clocks": bf["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -680,31 +757,33 @@ def served_workload(count, device):
     return jobs
 
 
-def run_served_form(args):
-    """Served form: the arrival stream through de_server (jobs overlapping on the
-    GPU) against the FP32 plain form running the same jobs one after another."""
+class ServedStart:
+    """Every job starts from a slice of one seeded U[-0.5, 0.5) pool."""
+
+    def __init__(self, jobs):
+        nmax = max(j["n"] for j in jobs)
+        self.pool = np.random.Generator(np.random.PCG64(1)).uniform(-0.5, 0.5, size=nmax * 128).astype(np.float32)
+
+    def __call__(self, j):
+        return self.pool[: j["n"] * j["dim"]].reshape(j["n"], j["dim"])
+
+
+def job_precision(j, precision):
+    """BF16 storage for the jobs the BF16 form takes (dim 64-256), FP32 otherwise."""
+    return "bf16" if precision == "bf16" and j["dim"] >= 64 else "fp32"
+
+
+def served_leg(jobs, x0_of, slots, precision, time_scale, local, clocks=False):
+    """The arrival stream through de_server with arrival times scaled by
+    `time_scale` (1: the configuration's 200 jobs/s): jobs overlap on the GPU as
+    slots and memory allow.  Returns latency percentiles and throughput."""
     import threading
 
-    import torch
-
     import distembed_gb300 as de
-    import oracle
-    torch.cuda.set_device(0)
-    t0 = time.perf_counter()
-    jobs = served_workload(args.jobs, "cuda")
-    gen_s = time.perf_counter() - t0
     B, ns, lr = W5["batch"], W5["ns"], W5["lr"]
-    nmax = max(j["n"] for j in jobs)
-    pool = np.random.Generator(np.random.PCG64(1)).uniform(-0.5, 0.5, size=nmax * 128).astype(np.float32)
-
-    def x0_of(j):  # every job starts from a slice of one seeded U[-0.5, 0.5) pool
-        return pool[: j["n"] * j["dim"]].reshape(j["n"], j["dim"])
-
-    srv = de.Server(slots=args.slots, hbm_fraction=0.85)
-    # warm-up: a few small jobs (module load, first launches)
-    small = sorted(jobs, key=lambda j: j["n"])[:4]
-    for j in small:
-        srv.wait(srv.submit(j["rowptr"], j["col"], x0_of(j), 2, B, ns, lr))
+    srv = de.Server(slots=slots, hbm_fraction=0.85, device=local)
+    for j in sorted(jobs, key=lambda j: j["n"])[:4]:  # warm-up: module load, first launches
+        srv.wait(srv.submit(j["rowptr"], j["col"], x0_of(j), 2, B, ns, lr, precision=job_precision(j, precision)))
     results = [None] * len(jobs)
     ids = [None] * len(jobs)
     ready = threading.Semaphore(0)
@@ -716,52 +795,97 @@ def run_served_form(args):
             results[i] = (float(loss[-1]), info)
 
     th = threading.Thread(target=waiter)
-    clocks = Clocks(0)
-    clocks.start()
+    clk_rec = Clocks(local) if clocks else None
+    if clk_rec:
+        clk_rec.start()
     th.start()
     start = srv.clock() + 0.05
     for i, j in enumerate(jobs):
-        delay = start + j["arrival"] - srv.clock()
+        delay = start + j["arrival"] * time_scale - srv.clock()
         if delay > 0:
             time.sleep(delay)
-        ids[i] = srv.submit(j["rowptr"], j["col"], x0_of(j), j["epochs"], B, ns, lr)
+        ids[i] = srv.submit(j["rowptr"], j["col"], x0_of(j), j["epochs"], B, ns, lr,
+                            precision=job_precision(j, precision))
         ready.release()
     th.join()
-    clk = clocks.stop()
+    clk = clk_rec.stop() if clk_rec else None
     st = srv.stats()
     srv.close()
-    lat = np.array([r[1]["end_s"] - (start + j["arrival"]) for r, j in zip(results, jobs)])
+    lat = np.array([r[1]["end_s"] - (start + j["arrival"] * time_scale) for r, j in zip(results, jobs)])
     queue_wait = np.array([r[1]["start_s"] - r[1]["submit_s"] for r in results])
     service = np.array([r[1]["end_s"] - r[1]["start_s"] for r in results])
     upd = sum(r[1]["edge_updates"] for r in results)
     makespan = max(r[1]["end_s"] for r in results) - start
-    value = upd / makespan
+    span = jobs[-1]["arrival"] * time_scale
+    return {"jobs": len(jobs), "rate_jobs_per_s": len(jobs) / span if span > 0 else None,
+            "offered_edge_updates_per_s": upd / span if span > 0 else None,
+            "edge_updates_per_s": upd / makespan, "makespan_s": makespan, "edge_updates": int(upd),
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max()), "queue_wait_p50": float(np.percentile(queue_wait, 50)),
+                          "queue_wait_p99": float(np.percentile(queue_wait, 99)),
+                          "service_p50": float(np.percentile(service, 50)),
+                          "service_p99": float(np.percentile(service, 99))},
+            "precision": {p: sum(job_precision(j, precision) == p for j in jobs) for p in ("bf16", "fp32")},
+            "slots": slots, "server": st, "clocks": clk, "final_loss": [r[0] for r in results]}
 
-    # the same jobs through the FP32 plain form, one after another (no overlap)
-    plain_s, plain_upd = 0.0, 0
-    for j in jobs:
-        with de.Handle(j["rowptr"], j["col"], j["dim"], quirks=True) as h:
-            h.set_embeddings(x0_of(j))
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            h.run(j["epochs"], B, ns, lr, want_loss=True)
-            plain_s += time.perf_counter() - t1
-            plain_upd += h.edge_updates(j["epochs"], B, ns)
-    plain_v = plain_upd / plain_s
 
-    # FP64 oracle on the three smallest kNN jobs (kNN training converges; small
-    # R-MAT jobs are chaotic, FP32 and FP64 trajectories part within tens of epochs)
-    small_knn = sorted((i for i in range(len(jobs)) if jobs[i]["kind"] == "knn"), key=lambda i: jobs[i]["n"])[:3]
-    oracle_gaps = []
-    for i in small_knn:
+def served_pair(jobs, x0_of, slots, precision, local):
+    """The stream at the configuration's rate and at half of the capacity that
+    rate measured (so that latency is service, not queueing)."""
+    full = served_leg(jobs, x0_of, slots, precision, 1.0, local, clocks=True)
+    scale = max(1.0, full["offered_edge_updates_per_s"] / (0.5 * full["edge_updates_per_s"]))
+    half = served_leg(jobs, x0_of, slots, precision, scale, local)
+    return full, half
+
+
+def served_oracle_gaps(jobs, x0_of, final_loss, count=3):
+    """FP64 oracle on the `count` smallest kNN jobs (kNN training converges; small
+    R-MAT jobs are chaotic, FP32 and FP64 trajectories part within tens of epochs)."""
+    import oracle
+    B, ns, lr = W5["batch"], W5["ns"], W5["lr"]
+    small = sorted((i for i in range(len(jobs)) if jobs[i]["kind"] == "knn"), key=lambda i: jobs[i]["n"])[:count]
+    out = []
+    for i in small:
         j = jobs[i]
         _, lo = oracle.run(j["rowptr"], j["col"], x0_of(j).astype(np.float64), j["epochs"], B, ns, lr, quirks=True,
                            threads=os.cpu_count() or 1)
-        oracle_gaps.append(abs(results[i][0] - lo[-1]) / lo[-1])
+        out.append({"job": i, "n": j["n"], "dim": j["dim"], "gap": float(abs(final_loss[i] - lo[-1]) / lo[-1])})
+    return out
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": len(small),
-            "ms_per_step": 1e3 * makespan, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32",
+
+def run_served_form(args):
+    """Served form: the arrival stream through de_server at the configuration's
+    rate and at half the measured capacity, against the FP32 plain form running
+    the same jobs one after another."""
+    import torch
+
+    import distembed_gb300 as de
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    jobs = served_workload(args.jobs, "cuda")
+    gen_s = time.perf_counter() - t0
+    B, ns, lr = W5["batch"], W5["ns"], W5["lr"]
+    x0_of = ServedStart(jobs)
+    full, half = served_pair(jobs, x0_of, args.slots, args.served_precision, 0)
+
+    # the same jobs through the FP32 plain form, one after another (no overlap)
+    plain_s, plain_upd = 0.0, 0
+    if not args.no_plain_compare:
+        for j in jobs:
+            with de.Handle(j["rowptr"], j["col"], j["dim"], quirks=True) as h:
+                h.set_embeddings(x0_of(j))
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                h.run(j["epochs"], B, ns, lr, want_loss=True)
+                plain_s += time.perf_counter() - t1
+                plain_upd += h.edge_updates(j["epochs"], B, ns)
+    gaps = [] if args.no_gap else served_oracle_gaps(jobs, x0_of, full["final_loss"])
+    for leg in (full, half):
+        leg.pop("final_loss")
+    value = full["edge_updates_per_s"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 4,
+            "ms_per_step": 1e3 * full["makespan_s"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.served_precision,
             "data": f"synthetic: {len(jobs)} jobs, Poisson arrivals {W5['rate']:.0f}/s (seed 4), n log-uniform "
                     "[1000, 2e6], R-MAT ef 8 or kNN k=10 (kNN up to 1e5 vertices), dim in {32, 64, 128}, "
                     "10-50 epochs; minibatch 16384, 5 negatives, lr 0.02",
@@ -770,20 +894,17 @@ def run_served_form(args):
                                                                      for k in ("knn", "rmat")},
                        "vertices": int(sum(jj["n"] for jj in jobs)), "nnz": int(sum(len(jj["col"]) for jj in jobs)),
                        "generate_s": round(gen_s, 1)},
-            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                          "max": float(lat.max()), "queue_wait_p50": float(np.percentile(queue_wait, 50)),
-                          "service_p50": float(np.percentile(service, 50)),
-                          "service_p99": float(np.percentile(service, 99))},
-            "server": st, "edge_updates": int(upd), "makespan_s": makespan,
-            "compare": {"fp32_plain_serial": {"edge_updates_per_s": plain_v, "busy_s": plain_s},
-                        "served_over_plain": value / plain_v},
-            "loss": {"final_gap_vs_fp64_oracle_3_smallest_knn_jobs": [float(g) for g in oracle_gaps],
+            "served_at_config_rate": full, "served_at_half_capacity": half,
+            "compare": {"fp32_plain_serial": {"edge_updates_per_s": plain_upd / plain_s if plain_s else None,
+                                              "busy_s": plain_s},
+                        "served_over_plain": value / (plain_upd / plain_s) if plain_s else None},
+            "loss": {"final_gap_vs_fp64_oracle_smallest_knn_jobs": gaps,
                      "served_vs_alone": "bitwise equal (tests/test_gpu_served.py)"},
             "e2e": {"value": value, "unit": UNIT,
-                    "h2d_bytes_per_step": int(sum(jj["n"] * jj["dim"] * 4 + len(jj["col"]) * 4 for jj in jobs)),
+                    "h2d_bytes_per_step": int(sum(jj["n"] * jj["dim"] * 4 + len(jj["col"]) * 8 for jj in jobs)),
                     "d2h_bytes_per_step": int(sum(jj["n"] * jj["dim"] * 4 for jj in jobs)),
                     "note": "jobs submitted from host memory and results returned to host memory by the server"},
-            "gpu_launches": None, "clocks": clk}
+            "gpu_launches": None, "clocks": full["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -982,10 +1103,185 @@ def run_sparse_form(args):
     print(json.dumps(line), flush=True)
 
 
+
+def run_reference(args):
+    """The reference's CPU algorithm (the FP64 port, -O3, every host core) on the
+    default line's workload: one step = one epoch of every graph (epoch k mod 20
+    of the job, state carried from step to step), one graph per thread.  The
+    graphs are generated as in the GPU arm (torch on the GPU when one is
+    present, so that both arms train the same graphs); nothing of this package
+    runs in the timed region."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    if args.form == "plain":
+        return run_reference_plain(args)
+    import oracle
+    try:
+        import torch
+        device = "cuda" if torch.cuda.is_available() else "cpu"
+    except ImportError:
+        device = None
+    graphs, x0 = batched_workload(args.graphs, device)
+    xs = [np.ascontiguousarray(x, dtype=np.float64) for x in x0]
+    csr = [(rp, c) for _, _, rp, c in graphs]
+    threads = os.cpu_count() or 1
+    E = W4["epochs"]
+
+    def step(k):
+        u, _ = oracle.run_many(csr, xs, 1, W4["batch"], W4["ns"], W4["lr"], first_epoch=k % E, want_loss=False,
+                               threads=threads, fast=True)
+        return u
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    updates = sum(step(args.warmup + k) for k in range(args.steps))
+    dt = time.perf_counter() - t0
+    v = updates / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": BATCHED_DATA.format(g=len(graphs)), "config": batched_config(graphs),
+            "impl_detail": {"step": "one epoch of every graph (epoch k mod 20 of the job)",
+                            "parallelism": "1 process x all host cores, one graph per thread",
+                            "graphs_generated_on": device},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "build": "g++ -O3 -ffp-contract=fast -fopenmp (oracle/liboracle_fast.so)",
+                             "sample": f"{args.steps} epochs of all {len(graphs)} graphs, FP64, {updates} edge-updates"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_plain(args):
+    """The FP64 port on the plain form's workload (R-MAT scale 20): one step =
+    one minibatch of epoch 0, OpenMP over its rows as the reference."""
+    import oracle
+    n, rowptr, col, x0 = workload()
+    batches = (n + W["batch"] - 1) // W["batch"]
+    x = np.array(x0, dtype=np.float64, copy=True)
+    threads = os.cpu_count() or 1
+
+    def step(k):
+        j = (37 * k) % batches
+        return oracle.run_batches(rowptr, col, x, 0, W["batch"], W["ns"], W["lr"], [j], quirks=True, threads=threads,
+                                  fast=True)
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    updates = sum(step(args.warmup + k) for k in range(args.steps))
+    dt = time.perf_counter() - t0
+    v = updates / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: R-MAT scale 20 (ef 16, a.57 b.19 c.19, seed 1), U[-0.5,0.5] init (seed 0)",
+            "config": {"workload": WORKLOAD, "n": n, "nnz": int(len(col)), "dim": W["dim"], "batch": W["batch"],
+                       "ns": W["ns"], "lr": W["lr"], "epochs_per_job": W["epochs"],
+                       "step": "one minibatch of epoch 0 (j = 37k mod 256)",
+                       "parallelism": "1 process x all host cores (OpenMP)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "build": "g++ -O3 -ffp-contract=fast -fopenmp (oracle/liboracle_fast.so)",
+                             "sample": f"{args.steps} minibatches, FP64, {updates} edge-updates"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_headline(args):
+    """The default line: the metric's comparison on the batched workload, the
+    other forms beside it (on rank 0 of a one-GPU run)."""
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    graphs, x0 = batched_workload(args.graphs, f"cuda:{local}")
+    gen_s = time.perf_counter() - t0
+    x0_all = np.concatenate(x0)
+    kinds = [k for k, _, _, _ in graphs]
+    shape = parse_shape(args.shape) if args.shape else None
+    if world > 1:
+        torch.distributed.barrier()
+    bf = batched_leg(graphs, x0_all, "bf16", local, args.steps, args.warmup, args.e2e_steps, shape=shape,
+                     clocks=True)
+    total_s = max_over_ranks(sum(bf["step_ms"]) / 1e3, world)
+    value = whole_job_rate(bf["edge_updates"] * args.steps, total_s, world)
+    e2e = bf["e2e"]
+    if e2e is not None and world > 1:
+        e2e_s = max_over_ranks(e2e["ms_per_step"] / 1e3, world)
+        e2e = dict(e2e, value=bf["edge_updates"] * world / e2e_s, ms_per_step=1e3 * e2e_s)
+    extras = rank == 0 and world == 1
+    compare, loss, cpu, served = {}, None, None, None
+    if extras:
+        f32 = batched_leg(graphs, x0_all, "fp32", local, max(1, args.steps // 4), 1, shape=bf["shape"])
+        compare["fp32_storage_batched"] = {"edge_updates_per_s": f32["value"],
+                                           "ms_per_step": statistics.mean(f32["step_ms"]), "shape": f32["shape"],
+                                           "note": "the same 512 graphs in the same persistent launch, FP32 storage"}
+        if not args.no_plain_compare:
+            compare["fp32_plain_same_graphs"] = plain_same_graphs(graphs, x0, local)
+        plain = plain_leg(args, rank, world, local, with_cpu=not args.no_cpu_baseline, with_gap=not args.no_gap)
+        for k in ("metric", "unit", "higher_is_better", "scaling", "vs_baseline", "n_gpus"):
+            plain.pop(k, None)
+        compare["fp32_plain_rmat20"] = plain
+        compare["bf16_batched_over_fp32_plain_same_graphs"] = (
+            value / compare["fp32_plain_same_graphs"]["edge_updates_per_s"]
+            if "fp32_plain_same_graphs" in compare else None)
+        compare["bf16_batched_over_fp32_plain_rmat20"] = value / plain["value"]
+        compare["bf16_batched_over_fp32_storage_batched"] = value / f32["value"]
+        if not args.no_gap:
+            lo = fp64_oracle_losses(graphs, x0)
+            loss = {"bf16_vs_fp64_oracle": gap_stats(bf["loss"], lo, kinds),
+                    "fp32_storage_vs_fp64_oracle": gap_stats(f32["loss"], lo, kinds),
+                    "oracle": "oracle/liboracle.so (bit-exact with the reference's own code), every graph's "
+                              "20-epoch job, loss of every epoch"}
+        if not args.no_cpu_baseline:
+            cpu = batched_cpu_baseline(graphs, x0, args.cpu_seconds)
+        if not args.no_served:
+            jobs = served_workload(args.jobs, f"cuda:{local}")
+            x0_of = ServedStart(jobs)
+            full, half = served_pair(jobs, x0_of, args.slots, args.served_precision, local)
+            gaps = [] if args.no_gap else served_oracle_gaps(jobs, x0_of, full["final_loss"])
+            for leg in (full, half):
+                leg.pop("final_loss")
+                leg.pop("clocks", None)
+            served = {"workload": f"served{len(jobs)}_poisson200: Poisson arrivals 200 jobs/s (seed 4), n "
+                                  "log-uniform [1000, 2e6], R-MAT ef 8 or kNN k=10 (kNN up to 1e5 vertices), dim in "
+                                  "{32, 64, 128}, 10-50 epochs, minibatch 16384, 5 negatives, lr 0.02",
+                      "storage": f"{args.served_precision} (dim 32 jobs FP32)",
+                      "at_config_rate": full, "at_half_capacity": half,
+                      "final_gap_vs_fp64_oracle_smallest_knn_jobs": gaps,
+                      "served_vs_alone": "bitwise equal (tests/test_gpu_served.py)"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": BATCHED_DATA.format(g=len(graphs)),
+                "config": batched_config(graphs),
+                "impl_detail": {"storage": "BF16 rows read, FP32 master, FP32 arithmetic, FP64 loss sums",
+                                "team_shape": bf["shape"], "autotune_s": round(bf["tune_s"], 2),
+                                "autotune_shapes": len(bf["tuned"]),
+                                "autotune_top3_ms": [[sh, round(t, 2)] for sh, t in
+                                                     sorted(bf["tuned"], key=lambda x: x[1])[:3]],
+                                "trace": bf["trace"], "generate_s": round(gen_s, 1),
+                                "step": "one launch: every graph, 20 epochs (CUDA graph)",
+                                "reset": "embeddings reset to the start values before every step (untimed)",
+                                "l2": "inputs larger than L2 (embeddings of every graph); no flush",
+                                "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roofline_batched(graphs, bf["step_ms"]),
+                "loss": loss, "compare": compare or None, "served": served,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": bf["clocks"]}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.form == "plain":
+        run_plain_form(args)
     elif args.form == "bf16":
         run_bf16_form(args)
     elif args.form == "batched":
@@ -997,7 +1293,7 @@ def main():
     elif args.form == "sparse":
         run_sparse_form(args)
     else:
-        run_ours(args)
+        run_headline(args)
 
 
 if __name__ == "__main__":

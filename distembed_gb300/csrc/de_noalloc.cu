@@ -26,7 +26,6 @@
 // pre-minibatch values as the reference's does.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/distembed_gb300.h"
@@ -40,7 +39,6 @@ namespace {
 constexpr int64_t kNoAllocMaxRowFloats = int64_t(1) << 20;  // 4 MiB of staged rows
 constexpr int64_t kNoAllocMaxRows = 65536;                  // loss partials (FP64)
 constexpr size_t kNoAllocBytes = size_t(kNoAllocMaxRowFloats) * sizeof(float) + size_t(kNoAllocMaxRows) * sizeof(double);
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -136,33 +134,18 @@ __global__ void __launch_bounds__(256) noalloc_commit_kernel(const NoAllocArgs a
   if (threadIdx.x == 0) *a.loss = red[0];
 }
 
-// Device address of the scratch array, looked up once per device (with that
-// device current) and then reused.
-std::mutex g_setup_mutex;
-void *g_scratch_ptr[kMaxDevices] = {};
-
+// Device address of the scratch array in the current device's context.  It is
+// looked up on every call (a lookup allocates nothing): after a device reset, or
+// under another context on the same device, the module is loaded again at a new
+// address, and a cached address would point at memory of the old context.
 int scratch_for_current_device(void **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
   if (e != cudaSuccess) {
-    de::set_thread_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    de::set_thread_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     return DE_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    de::set_thread_error("device ordinal beyond the supported range");
-    return DE_ERR_UNSUPPORTED;
-  }
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void *ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      de::set_thread_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return DE_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = ptr;
-  }
-  *out = g_scratch_ptr[dev];
+  *out = ptr;
   return DE_OK;
 }
 

@@ -134,10 +134,11 @@ void de_negatives(int64_t n, int32_t seed, int32_t ns, int64_t *out);
  * rep_rows: leading rows of the minibatch that take the repulsive pass;
  * skip_last_vertex: 1 drops edges into vertex n-1 as the reference does.  Work
  * memory is a fixed device array of the library: batch rows * dim <= 1,048,576.
- * Larger minibatches return DE_ERR_INVALID (text in de_last_error(NULL)).  The
- * first call on a device looks that array up (cudaGetSymbolAddress), so make it
- * before any stream capture.  Calls share the array: calls that overlap on the
- * GPU race.  Launches on `stream` (a cudaStream_t, NULL = default stream) and
+ * Larger minibatches return DE_ERR_INVALID (text in de_last_error(NULL)).  Every
+ * call looks that array's address up in the current context
+ * (cudaGetSymbolAddress), so a new context after a device reset is followed; the
+ * first call on a device also loads the module, so make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.  Launches on `stream` (a cudaStream_t, NULL = default stream) and
  * returns without waiting. */
 int de_minibatch_noalloc(int64_t n, const int32_t *rowptr, const int32_t *col, int32_t dim, float *x,
                          int32_t batch_id, int32_t batch_size, const int32_t *negs, int32_t ns,

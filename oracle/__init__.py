@@ -4,8 +4,11 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
 checker and by bench.py's CPU legs.  The product (distembed_gb300) never
 imports it.
 
-Two libraries live here:
-  liboracle.so       the FP64 restatement (de_oracle.cpp), built anywhere g++ exists
+Three libraries live here:
+  liboracle.so       the FP64 restatement (de_oracle.cpp), built anywhere g++ exists;
+                     bit-exact with the reference (no fused multiply-add)
+  liboracle_fast.so  the same source built -O3 with contraction: the timed CPU
+                     baseline (FP64, not bit-exact)
   _ref/libderef.so   the reference's own code compiled against oracle/shim/; it can
                      only be built where the reference sources are (see Makefile)
 """
@@ -19,6 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
+_FAST = None
 _REF = None
 
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -37,29 +41,45 @@ def build(ref: bool = False) -> None:
 def lib():
     global _LIB
     if _LIB is None:
-        path = os.path.join(HERE, "liboracle.so")
-        src = os.path.join(HERE, "de_oracle.cpp")
-        if not os.path.exists(path) or os.path.getmtime(src) > os.path.getmtime(path):
-            build()
-        L = ctypes.CDLL(path)
-        L.oracle_negatives.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _i64p]
-        L.oracle_rep_rows.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
-        L.oracle_batch_grad.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
-                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
-                                        ctypes.c_int, ctypes.c_int, _f64p, _f64p]
-        L.oracle_run.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
-                                 ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int]
-        L.oracle_run_batches.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
-                                         ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
-                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int]
-        L.oracle_run_batches.restype = ctypes.c_int64
-        L.oracle_spmm.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_double, ctypes.c_int,
-                                  _f64p]
-        L.oracle_sparse_embedding.argtypes = [ctypes.c_int, ctypes.c_int64, _i64p, _i64p, _f64p, ctypes.c_int,
-                                              ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                                              ctypes.c_int, ctypes.c_int, _f64p]
-        _LIB = L
+        _LIB = _load("liboracle.so")
     return _LIB
+
+
+def lib_fast():
+    """The -O3 build of the same restatement (the timed CPU baseline)."""
+    global _FAST
+    if _FAST is None:
+        _FAST = _load("liboracle_fast.so")
+    return _FAST
+
+
+def _load(name):
+    path = os.path.join(HERE, name)
+    src = os.path.join(HERE, "de_oracle.cpp")
+    if not os.path.exists(path) or os.path.getmtime(src) > os.path.getmtime(path):
+        build()
+    L = ctypes.CDLL(path)
+    L.oracle_negatives.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, _i64p]
+    L.oracle_rep_rows.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.oracle_batch_grad.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, _f64p, _f64p]
+    L.oracle_run.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                             ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int]
+    L.oracle_run_batches.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int]
+    L.oracle_run_batches.restype = ctypes.c_int64
+    L.oracle_spmm.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_double, ctypes.c_int,
+                              _f64p]
+    L.oracle_sparse_embedding.argtypes = [ctypes.c_int, ctypes.c_int64, _i64p, _i64p, _f64p, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int, _f64p]
+    L.oracle_run_many.argtypes = [ctypes.c_int, _i64p, ctypes.POINTER(_i64p), ctypes.POINTER(_i64p), ctypes.c_int,
+                                  ctypes.POINTER(_f64p), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  _f64p, ctypes.c_int, _f64p, ctypes.c_int]
+    L.oracle_run_many.restype = ctypes.c_int64
+    return L
 
 
 def ref_path() -> str:
@@ -136,6 +156,33 @@ def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0):
     return x, loss[:epochs]
 
 
+def run_many(graphs, xs, epochs, batch, ns, lr, first_epoch=0, quirks=True, want_loss=True, threads=0,
+             fast=False):
+    """Many independent graphs, each one job of the one-rank step, spread over
+    `threads` host threads (one graph per thread at a time).  graphs: a list of
+    (rowptr, col); xs: their FP64 embeddings (n x dim, C-contiguous), updated in
+    place; epochs [first_epoch, first_epoch + epochs) with one lr per epoch.
+    Returns (edge-updates, loss [graphs, epochs] or None).  fast: the -O3 build
+    (the timed baseline) instead of the bit-exact one."""
+    L = lib_fast() if fast else lib()
+    csr = [_csr(rp, c) for rp, c in graphs]
+    for x in xs:
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+    G = len(graphs)
+    dim = xs[0].shape[1]
+    n = np.array([len(rp) - 1 for rp, _ in csr], dtype=np.int64)
+    rps = (_i64p * G)(*[_p(rp, _i64p) for rp, _ in csr])
+    cols = (_i64p * G)(*[_p(c, _i64p) for _, c in csr])
+    xps = (_f64p * G)(*[_p(x, _f64p) for x in xs])
+    lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+    loss = np.zeros((G, max(epochs, 1)), dtype=np.float64) if want_loss else None
+    u = L.oracle_run_many(G, _p(n, _i64p), rps, cols, dim, xps, first_epoch, epochs, batch, ns, _p(lrs, _f64p),
+                          int(quirks), _p(loss, _f64p), threads)
+    if u < 0:
+        raise ValueError("oracle_run_many failed")
+    return int(u), (loss[:, :epochs] if want_loss else None)
+
+
 def spmm(rowptr, col, x, lr, quirks=True):
     """The reference's SpMM step (cpp/algo/spmm.hpp:54-159): y = lr * A x, FP64."""
     rowptr, col = _csr(rowptr, col)
@@ -148,13 +195,14 @@ def spmm(rowptr, col, x, lr, quirks=True):
     return y
 
 
-def run_batches(rowptr, col, x, epoch_in_call, batch, ns, lr, batch_ids, quirks=True, threads=0):
+def run_batches(rowptr, col, x, epoch_in_call, batch, ns, lr, batch_ids, quirks=True, threads=0, fast=False):
     """Runs the listed minibatches of one epoch in place on x (FP64, C-contiguous);
-    returns the edge-updates performed.  Used for bounded CPU timing samples."""
+    returns the edge-updates performed.  Used for bounded CPU timing samples
+    (fast: the -O3 build)."""
     ids = np.ascontiguousarray(batch_ids, dtype=np.int32)
     n, dim = x.shape
     assert x.dtype == np.float64 and x.flags.c_contiguous
-    u = lib().oracle_run_batches(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epoch_in_call, batch,
+    u = (lib_fast() if fast else lib()).oracle_run_batches(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epoch_in_call, batch,
                                  ns, lr, int(quirks), _p(ids, ctypes.POINTER(ctypes.c_int32)), len(ids), threads)
     if u < 0:
         raise ValueError("oracle_run_batches failed")

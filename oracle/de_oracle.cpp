@@ -72,7 +72,7 @@ struct Batch {
 
 // Attractive pass for one source row (algo.hpp:531-582).  Returns the FP64
 // attractive loss of the row.
-inline double attract_row(const Batch &b, int64_t i, double *prev_row, double *fd) {
+inline double attract_row(const Batch &b, int64_t i, double *prev_row, double *fd, bool want_loss) {
   const int D = b.dim;
   const int64_t dst_end = b.quirks ? b.n - 1 : b.n;  // F7
   double loss = 0.0;
@@ -89,14 +89,14 @@ inline double attract_row(const Batch &b, int64_t i, double *prev_row, double *f
       double l = clip(fd[d] * d1);
       prev_row[d] = prev_row[d] + (b.lr) * l;
     }
-    loss += std::log1p(attrc);
+    if (want_loss) loss += std::log1p(attrc);
   }
   return loss;
 }
 
 // Repulsive pass for one row (algo.hpp:594-647).
 inline double repulse_row(const Batch &b, int64_t row, const int64_t *negs, int ns,
-                          double *prev_row, double *fd) {
+                          double *prev_row, double *fd, bool want_loss) {
   const int D = b.dim;
   double loss = 0.0;
   for (int k = 0; k < ns; ++k) {
@@ -112,7 +112,7 @@ inline double repulse_row(const Batch &b, int64_t row, const int64_t *negs, int 
       fd[d] = clip(fd[d] * d1);
       prev_row[d] += (b.lr) * fd[d];
     }
-    loss += std::log((1.0 + repuls) / (repuls + 0.000001));
+    if (want_loss) loss += std::log((1.0 + repuls) / (repuls + 0.000001));
   }
   return loss;
 }
@@ -131,15 +131,69 @@ void batch_grad(const Batch &b, const int64_t *negs, int ns, int rep_rows, doubl
     std::vector<double> fd(D);
 #pragma omp for schedule(static)
     for (int64_t i = src_begin; i < src_end; ++i) {
-      double l = attract_row(b, i, prev + (i - src_begin) * D, fd.data());
+      double l = attract_row(b, i, prev + (i - src_begin) * D, fd.data(), row_loss != nullptr);
       if (row_loss) row_loss[i - src_begin] = l;
     }
 #pragma omp for schedule(static)
     for (int64_t i = 0; i < rep_rows; ++i) {
-      double l = repulse_row(b, src_begin + i, negs, ns, prev + i * D, fd.data());
+      double l = repulse_row(b, src_begin + i, negs, ns, prev + i * D, fd.data(), row_loss != nullptr);
       if (row_loss && i < rows) row_loss[i] += l;
     }
   }
+}
+
+// Rows of minibatch j that receive the repulsive pass in epoch `epoch` (F8:
+// from the second epoch on, last_batch_size; algo.hpp:135, 167-169, 594).
+int rep_rows_of(int64_t n, int batch, int epoch, int batch_id, bool quirks) {
+  const int batches = int(n / batch) + (n % batch ? 1 : 0);
+  const int last = (n % batch) ? int(n - int64_t(batch) * (batches - 1)) : batch;
+  if (batch_id == batches - 1) return last;
+  if (quirks && epoch > 0) return last;
+  return batch;
+}
+
+// One graph's epochs [first_epoch, first_epoch + epochs) on one thread: the
+// same minibatch loop as oracle_run (seed = epoch + batch, attractive pass,
+// repulsive pass, update), the passes run row after row.  loss (nullable) gets
+// each epoch's FP64 loss; returns the edge-updates performed.
+int64_t run_graph_serial(int64_t n, const int64_t *rowptr, const int64_t *col, int dim, double *x,
+                         int first_epoch, int epochs, int batch, int ns, const double *lr_per_epoch,
+                         bool quirks, double *loss) {
+  const int batches = int(n / batch) + (n % batch ? 1 : 0);
+  std::vector<double> prev(static_cast<size_t>(batch) * dim);
+  std::vector<double> fd(static_cast<size_t>(dim)), row_loss(static_cast<size_t>(batch));
+  std::vector<int64_t> negs(size_t(std::max(ns, 1)));
+  const int64_t dst_end = quirks ? n - 1 : n;
+  int64_t updates = 0;
+  for (int i = 0; i < epochs; ++i) {
+    const int epoch = first_epoch + i;
+    double epoch_loss = 0.0;
+    for (int j = 0; j < batches; ++j) {
+      negatives(n, epoch + j, ns, negs.data());
+      Batch b{n, rowptr, col, dim, x, batch, j, lr_per_epoch[i], quirks};
+      const int rep_rows = rep_rows_of(n, batch, epoch, j, quirks);
+      const int64_t base = int64_t(j) * batch;
+      const int64_t rows = std::min<int64_t>(base + batch, n) - base;
+      std::fill(prev.begin(), prev.end(), 0.0);
+      for (int64_t r = 0; r < rows; ++r) {
+        row_loss[r] = attract_row(b, base + r, prev.data() + r * dim, fd.data(), loss != nullptr);
+        for (int64_t e = rowptr[base + r]; e < rowptr[base + r + 1]; ++e) updates += (col[e] >= 0 && col[e] < dst_end);
+      }
+      int valid = 0;
+      for (int k = 0; k < ns; ++k) valid += (negs[k] >= 0 && negs[k] < n);
+      for (int64_t r = 0; r < rep_rows; ++r) {
+        const double l = repulse_row(b, base + r, negs.data(), ns, prev.data() + r * dim, fd.data(), loss != nullptr);
+        if (r < rows) row_loss[r] += l;
+      }
+      updates += int64_t(rep_rows) * valid;
+      for (int64_t r = 0; r < rows; ++r)
+        for (int d = 0; d < dim; ++d) x[(base + r) * dim + d] += prev[r * dim + d];
+      if (loss)  // row by row, as oracle_run sums it
+        for (int64_t r = 0; r < rows; ++r) epoch_loss += row_loss[r];
+    }
+    if (loss) loss[i] = epoch_loss;
+  }
+  return updates;
 }
 
 }  // namespace
@@ -240,6 +294,37 @@ int64_t oracle_run_batches(int64_t n, const int64_t *rowptr, const int64_t *col,
     updates += int64_t(rep_rows) * valid;
   }
   return updates;
+}
+
+/* Many independent graphs, each one job of the one-rank step (the loop of
+ * oracle_run, epochs [first_epoch, first_epoch + epochs) with the seeds and
+ * repulsive row counts of those epochs), the graphs spread over `threads`
+ * threads (largest first; a graph runs on one thread, its minibatches in
+ * order).  x[g] is graph g's embedding (n[g] x dim, FP64), updated in place;
+ * loss (nullable) gets [n_graphs x epochs] FP64 losses, and with loss NULL no
+ * logarithm is taken.  Returns the edge-updates performed, or -1. */
+int64_t oracle_run_many(int n_graphs, const int64_t *n, const int64_t *const *rowptr, const int64_t *const *col,
+                        int dim, double *const *x, int first_epoch, int epochs, int batch, int ns,
+                        const double *lr_per_epoch, int quirks, double *loss, int threads) {
+  if (n_graphs < 0 || dim <= 0 || batch <= 0 || ns < 0 || epochs < 0 || first_epoch < 0) return -1;
+  for (int g = 0; g < n_graphs; ++g)
+    if (n[g] <= 0) return -1;
+  std::vector<int> order(static_cast<size_t>(n_graphs));
+  for (int g = 0; g < n_graphs; ++g) order[g] = g;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return n[a] + rowptr[a][n[a]] > n[b] + rowptr[b][n[b]];
+  });
+  int64_t total = 0;
+#ifdef _OPENMP
+  const int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt) reduction(+ : total)
+#endif
+  for (int t = 0; t < n_graphs; ++t) {
+    const int g = order[t];
+    total += run_graph_serial(n[g], rowptr[g], col[g], dim, x[g], first_epoch, epochs, batch, ns, lr_per_epoch,
+                              quirks != 0, loss ? loss + size_t(g) * epochs : nullptr);
+  }
+  return total;
 }
 
 /* SpMMAlgo::algo_spmm at one rank (cpp/algo/spmm.hpp:54-159): for every row i,

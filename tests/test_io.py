@@ -106,6 +106,59 @@ void f(SpMat *s, DenseMat *d, Grid *g) {
     assert r.returncode == 0, r.stderr
 
 
+def _ref_root():
+    return os.environ.get("DE_REF_ROOT") or os.path.abspath(os.path.join(ROOT, "..", "reference"))
+
+
+def test_cpp_header_compiles_against_the_reference_headers(tmp_path):
+    # the binding as the reference driver's embedding branch would use it
+    # (cpp/dist_embed.cpp:331-346, only the class name changed), compiled against
+    # the reference's own SpMat / DenseMat / Process3DGrid headers where they lie,
+    # with oracle/shim/ standing in for MPI, MKL and Eigen (the include path of
+    # oracle/Makefile's `ref` target)
+    ref = _ref_root()
+    if not os.path.exists(os.path.join(ref, "cpp", "core", "sparse_mat.hpp")):
+        pytest.skip("reference sources not present")
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_ROOT={ref}"],
+                          stderr=subprocess.DEVNULL)
+    src = tmp_path / "embedding_branch.cpp"
+    src.write_text('''
+#include "algo/algo.hpp"
+#include "core/dense_mat.hpp"
+#include "core/sparse_mat.hpp"
+#include "net/process_3D_grid.hpp"
+#include "distembed_gb300.hpp"
+#include <memory>
+using namespace std;
+using namespace distblas::core;
+using namespace distblas::net;
+void embedding_branch(Process3DGrid *grid, shared_ptr<SpMat<VALUE_TYPE>> shared_sparseMat,
+                      shared_ptr<SpMat<VALUE_TYPE>> shared_sparseMat_receiver,
+                      shared_ptr<SpMat<VALUE_TYPE>> shared_sparseMat_sender, INDEX_TYPE localARows, double alpha,
+                      double beta, bool col_major, bool sync_comm, int iterations, int batch_size, int ns,
+                      VALUE_TYPE lr) {
+  const int dimension = 128;
+  auto dense_mat = shared_ptr<DenseMat<INDEX_TYPE, VALUE_TYPE, dimension>>(
+      new DenseMat<INDEX_TYPE, VALUE_TYPE, dimension>(grid, localARows));
+  unique_ptr<distembed_gb300::GpuEmbeddingAlgo<INDEX_TYPE, VALUE_TYPE, dimension>> embedding_algo =
+      make_unique<distembed_gb300::GpuEmbeddingAlgo<INDEX_TYPE, VALUE_TYPE, dimension>>(
+          shared_sparseMat.get(), shared_sparseMat_receiver.get(), shared_sparseMat_sender.get(),
+          dense_mat.get(), grid, alpha, beta, 5, -5, col_major, sync_comm);
+  embedding_algo->algo_force2_vec_ns(iterations, batch_size, ns, lr);
+}
+''')
+    ovl = os.path.join(ROOT, "oracle", "_ref", "overlay")
+    gxx = subprocess.run(["g++", "-dumpversion"], capture_output=True, text=True).stdout.strip().split(".")[0]
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", "-w", "-fpermissive", "-include", "climits", "-I-",
+           "-I" + os.path.join(ROOT, "oracle", "shim"), "-I" + os.path.join(ovl, "algo"),
+           "-I" + os.path.join(ref, "cpp", "algo"), "-I" + os.path.join(ovl, "core"),
+           "-I" + os.path.join(ref, "cpp", "core"), "-I" + os.path.join(ref, "cpp"),
+           "-I" + os.path.join(ref, "cpp", "net"), f"-I/usr/include/c++/{gxx}/pstl",
+           "-I" + os.path.join(ROOT, "include"), str(src)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+
+
 def _big_file(path, n, m, seed, bad_at=None, extra=0):
     """A general file of m random entries over n vertices, comment lines every
     1000 entries, optionally a malformed entry line at index bad_at and `extra`
