@@ -394,8 +394,15 @@ def run_bf16_form(args):
     batches = -(-n // B)
     out, clk, e2e = {}, None, None
     names = {0: "minibatch/attractive", 1: "repulsion_gemm", 2: "update_exact_rows", 3: "flush", 4: "negative_gather"}
+    final_x = {}
     for form in ("fp32", "bf16"):
-        h = de.Handle(rowptr, col, dim, precision=form, quirks=True, compute_loss=True, pdl=bool(args.pdl))
+        # the same job twice: timed on a handle that computes no loss (the
+        # reference computes none), then again on one that does, for the losses
+        with de.Handle(rowptr, col, dim, precision=form, quirks=True, compute_loss=True, pdl=bool(args.pdl)) as hl:
+            hl.set_embeddings(x0)
+            loss = hl.run(E, B, ns, lr, want_loss=True)
+            final_x[form] = hl.get_embeddings()
+        h = de.Handle(rowptr, col, dim, precision=form, quirks=True, compute_loss=False, pdl=bool(args.pdl))
         stream = torch.cuda.ExternalStream(h.stream, device=0)
         h.set_embeddings(x0)
         upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
@@ -405,8 +412,6 @@ def run_bf16_form(args):
         ms = timed_job(h, E, B, ns, lr, stream, warmup=1)
         if form == "bf16":
             clk = clocks.stop()
-        h.set_embeddings(x0)
-        loss = h.run(E, B, ns, lr, want_loss=True)   # the same job, for its losses
         pms, kind = h.profile_epoch(B, ns, lr)      # one more epoch, an event around every launch
         out[form] = {"edge_updates_per_s": sum(upd) / (sum(ms) / 1e3), "ms_per_epoch": statistics.mean(ms),
                      "loss_per_epoch": [float(v) for v in loss],
@@ -455,6 +460,20 @@ def run_bf16_form(args):
                  "note": "per CSR entry: column id + BF16 neighbour row; per vertex: rowptr, own BF16 row, FP32 update row"}
     dominant_gemm = prof["repulsion_gemm"] >= prof["minibatch/attractive"]
     gap = abs(out["bf16"]["loss_per_epoch"][-1] - out["fp32"]["loss_per_epoch"][-1]) / out["fp32"]["loss_per_epoch"][-1]
+    # every epoch against the FP64 oracle: the GPU restatement (bitwise the CPU
+    # oracle's arithmetic, tests/test_gpu_oracle64.py), same FP32-rounded start
+    fp64 = None
+    if not args.no_gap:
+        import oracle
+        t1 = time.perf_counter()
+        xo, lo = oracle.gpu_run(rowptr, col, x0.astype(np.float64), E, B, ns, lr, quirks=True)
+        fp64 = {"oracle": "oracle/liboracle_gpu.so (FP64, bitwise the CPU oracle on small graphs)",
+                "oracle_s": round(time.perf_counter() - t1, 1), "loss_per_epoch": [float(v) for v in lo]}
+        for form in ("bf16", "fp32"):
+            lg = np.asarray(out[form]["loss_per_epoch"])
+            fp64[form] = {"loss_rel_per_epoch": [float(v) for v in np.abs(lg - lo) / lo],
+                          "loss_rel_max": float(np.max(np.abs(lg - lo) / lo)),
+                          "x_rel_l2_final": float(np.linalg.norm(final_x[form] - xo) / np.linalg.norm(xo))}
     line = {"metric": METRIC, "value": out["bf16"]["edge_updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": E,
             "warmup": 1, "ms_per_step": out["bf16"]["ms_per_epoch"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16",
@@ -467,7 +486,8 @@ def run_bf16_form(args):
             "e2e": e2e, "clocks": clk, "gpu_launches": E * (4 * batches + 1),
             "compare": {"fp32_plain": {k: v for k, v in out["fp32"].items()}, "bf16": out["bf16"],
                         "bf16_over_fp32": out["bf16"]["edge_updates_per_s"] / out["fp32"]["edge_updates_per_s"],
-                        "final_loss_gap_vs_fp32": gap}}
+                        "final_loss_gap_vs_fp32": gap},
+            "gap_vs_fp64_oracle": fp64}
     print(json.dumps(line), flush=True)
 
 W4 = dict(n_lo=500, n_hi=50000, seed=3, dim=64, batch=256, ns=5, lr=0.02, epochs=20, init_seed=1000,
@@ -547,8 +567,12 @@ def batched_leg(graphs, x0_all, precision, local, steps, warmup, e2e_steps=0, sh
     b.prepare(E, B, ns, lr)
     b.set_embeddings(-1, x_start)
     b.launch()
-    loss = b.wait()
+    loss = b.wait()            # the job's loss, every epoch (for the oracle comparison)
     trace = b.trace()
+    # the timed launches compute the loss of the job's last epoch only (the one
+    # the metric's loss gap is taken on); the other epochs take no logarithm
+    b.set_loss("last")
+    b.prepare(E, B, ns, lr)
     for _ in range(warmup):
         b.set_embeddings(-1, x_start)
         b.launch()
@@ -580,7 +604,7 @@ def batched_leg(graphs, x0_all, precision, local, steps, warmup, e2e_steps=0, sh
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             b.set_embeddings(-1, x_host)
-            b.run(E, B, ns, lr)
+            e2e_loss = b.run(E, B, ns, lr)
             b.get_embeddings(-1, out=out_host)
             if k > 0:
                 ts.append(time.perf_counter() - t1)
@@ -590,11 +614,12 @@ def batched_leg(graphs, x0_all, precision, local, steps, warmup, e2e_steps=0, sh
                "d2h_bytes_per_step": total_n * dim * 4 + len(graphs) * E * 8,
                "ms_per_step": 1e3 * statistics.mean(ts),
                "step": "host FP32 embeddings of every graph in (pinned), de_batch_run (host sampler, draws "
-                       "uploaded, graph captured, the 20-epoch launch, losses back), host FP32 out"}
+                       "uploaded, graph captured, the 20-epoch launch, final-epoch losses back), host FP32 out",
+               "final_loss_equal_to_timed_job": bool(np.array_equal(e2e_loss[:, -1], loss[:, -1]))}
         b.prepare(E, B, ns, lr)
     b.close()
     span = trace[:, 1] - trace[:, 0]
-    return {"edge_updates": upd, "step_ms": step_ms, "value": upd / (sum(step_ms) / 1e3), "loss": loss,
+    return {"edge_updates": upd, "step_ms": step_ms, "value": upd * len(step_ms) / (sum(step_ms) / 1e3), "loss": loss,
             "shape": shape, "tuned": tuned, "tune_s": tune_s, "e2e": e2e, "clocks": clk,
             "trace": {"makespan_ms": float(trace[:, 1].max()) / 1e6, "longest_graph_ms": float(span.max()) / 1e6,
                       "graph_ms_sum": float(span.sum()) / 1e6, "teams": int(len(np.unique(trace[:, 2])))}}

@@ -35,7 +35,7 @@ EXPORTS = ("de_default_options", "de_create", "de_destroy", "de_set_embeddings",
            "de_edge_updates",
            "de_negatives", "de_minibatch_noalloc", "de_stream", "de_last_error", "de_version",
            "de_batch_create", "de_batch_destroy", "de_batch_set_embeddings_f32", "de_batch_get_embeddings_f32",
-           "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_trace", "de_batch_stream",
+           "de_batch_set_shape", "de_batch_get_shape", "de_batch_prepare", "de_batch_launch", "de_batch_wait", "de_batch_run", "de_batch_autotune", "de_batch_edge_updates", "de_batch_set_near_distance", "de_batch_set_loss", "de_batch_trace", "de_batch_stream",
            "de_batch_last_error", "de_server_create", "de_server_submit", "de_server_info", "de_server_wait",
            "de_server_drain", "de_server_get_stats", "de_server_clock", "de_server_destroy", "de_server_last_error",
            "de_mm_read", "de_embedding_write", "de_mm_read_gpu", "de_coo_to_csr", "de_csr_info", "de_csr_copy",
@@ -145,6 +145,7 @@ def lib():
         L.de_batch_edge_updates.argtypes = [_vp, _i32, _i32, _i32]
         L.de_batch_edge_updates.restype = _i64
         L.de_batch_set_near_distance.argtypes = [_vp, ctypes.c_float]
+        L.de_batch_set_loss.argtypes = [_vp, _i32]
         L.de_batch_trace.argtypes = [_vp, _vp]
         L.de_batch_stream.argtypes = [_vp]
         L.de_batch_stream.restype = _vp
@@ -575,6 +576,10 @@ class Batch:
 
     def set_near_distance(self, near_r: float):
         self._check(lib().de_batch_set_near_distance(self._h, near_r))
+
+    def set_loss(self, mode: str):
+        """"every" (default), "last" (the last epoch of each run only) or "none"."""
+        self._check(lib().de_batch_set_loss(self._h, {"none": 0, "every": 1, "last": 2}[mode]))
 
     def trace(self) -> np.ndarray:
         """(graphs, 3): start and end (ns, from the earliest start) and team of each graph."""

@@ -157,6 +157,7 @@ struct de_batch {
   cudaGraphExec_t exec = nullptr;  // the prepared run
   int prepared_epochs = 0;
   float near_r = 0.02f;            // BF16 form: squared distance below which a pair is recomputed in FP32
+  int loss_mode = DE_LOSS_EVERY_EPOCH;
   long long *d_trace = nullptr;    // [n_graphs x 3] of the last launch
 };
 
@@ -376,7 +377,8 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   a.batch = B;
   a.ns = ns;
   a.quirks = b->opt.ref_quirks;
-  a.compute_loss = 1;
+  a.compute_loss = b->loss_mode != DE_LOSS_NONE;
+  a.loss_from = b->loss_mode == DE_LOSS_LAST_EPOCH ? epochs - 1 : 0;
   a.bound = float(b->opt.max_bound);
   a.stage = b->d_stage;
   a.slots = b->d_slots;
@@ -698,6 +700,7 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
     if (!pick_kernel(b->dim, bf16, sh, ns).fn) continue;
     rc = prepare_batched(b, epochs, batch_size, ns, lrs.data(), sh);
     if (rc) break;
+    b->args.compute_loss = 0;  // shapes are timed on the training work alone
     e = cudaMemcpyAsync(b->d_xm, save_m, xn * sizeof(float), cudaMemcpyDeviceToDevice, b->stream);
     if (e == cudaSuccess && b->d_xb)
       e = cudaMemcpyAsync(b->d_xb, save_b, xn * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, b->stream);
@@ -735,6 +738,16 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
   b->shape = best_shape;
   if (count) *count = tried;
   if (best) *best = best_shape;
+  return DE_OK;
+}
+
+int de_batch_set_loss(de_batch *b, int32_t mode) {
+  if (!b || (mode != DE_LOSS_NONE && mode != DE_LOSS_EVERY_EPOCH && mode != DE_LOSS_LAST_EPOCH))
+    return bfail(b, DE_ERR_INVALID, "loss mode must be DE_LOSS_NONE, DE_LOSS_EVERY_EPOCH or DE_LOSS_LAST_EPOCH");
+  b->loss_mode = mode;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->prepared_epochs = 0;
   return DE_OK;
 }
 

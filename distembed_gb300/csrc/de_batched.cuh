@@ -63,6 +63,7 @@ struct BatchedArgs {
   int32_t *cluster_slot;     // [clusters] graph handed from CTA rank 0 to rank 1
   float *item_loss;          // [teams, max items of a minibatch] loss of every work item
   int32_t item_stride;
+  int32_t loss_from;         // epochs e >= loss_from (of this run) compute their loss; the others write 0
 };
 
 static __device__ __forceinline__ long long globaltimer() {

@@ -54,7 +54,7 @@ __device__ __forceinline__ float group_sum(float v) {
 template <int D, int VPW, bool kBF16, bool kAttract>
 __device__ __forceinline__ void group_forces(const BatchedArgs &a, Row<D, VPW> &acc, const Row<D, VPW> &xi,
                                              int64_t voff, int ids, int k, int gbase, int gl, float lr,
-                                             float &loss) {
+                                             float &loss, bool want) {
   constexpr int L = Row<D, VPW>::L, P = Row<D, VPW>::P;
   constexpr int U = L >= 4 ? 4 : L;
   Row<D, VPW> xn[U];
@@ -107,7 +107,7 @@ __device__ __forceinline__ void group_forces(const BatchedArgs &a, Row<D, VPW> &
     if (nid[u] < 0) c = 0.f;
 #pragma unroll
     for (int t = 0; t < P; ++t) acc.v[t] = fmaf(lr, bclip((xi.v[t] - xn[u].v[t]) * c, a.bound), acc.v[t]);
-    if (nid[u] >= 0 && gl == 0) loss += kAttract ? log1pf(r[u]) : logf((1.0f + r[u]) / (r[u] + 1e-6f));
+    if (want && nid[u] >= 0 && gl == 0) loss += kAttract ? log1pf(r[u]) : logf((1.0f + r[u]) / (r[u] + 1e-6f));
   }
 }
 
@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(WARPS * 32) batched_kernel(const BatchedArgs a
     const int skip = skip_last ? G.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
     for (int e = 0; e < a.epochs; ++e) {
       const float lr = a.lr[e];
+      const bool want = a.compute_loss && e >= a.loss_from;
       double wloss = 0.0;  // this warp's share of the epoch loss, in item order
       for (int j = 0; j < G.batches; ++j) {
         const int64_t bi = G.batch_off + j;
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(WARPS * 32) batched_kernel(const BatchedArgs a
               if (ids == skip) ids = -1;
             }
             for (int k = 0; k < L && c0 + k < maxcnt; k += (L >= 4 ? 4 : L))
-              group_forces<D, VPW, kBF16, true>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss);
+              group_forces<D, VPW, kBF16, true>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss, want);
           }
           const bool repulse = has && it.part == 0 && it.row < rep_rows;
           const bool any_rep = __any_sync(kAll, repulse);
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(WARPS * 32) batched_kernel(const BatchedArgs a
               if (ids >= G.n) ids = -1;  // a draw equal to n contributes nothing
             }
             for (int k = 0; k < L && k0 + k < a.ns; k += (L >= 4 ? 4 : L))
-              group_forces<D, VPW, kBF16, false>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss);
+              group_forces<D, VPW, kBF16, false>(a, acc, xi, G.voff, ids, k, gbase, gl, lr, loss, want);
           }
           if (has) {
             float *dst = it.nparts > 1 ? slots + size_t(it.first_slot + it.part) * D : stage + size_t(it.row) * D;

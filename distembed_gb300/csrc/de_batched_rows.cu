@@ -21,7 +21,7 @@ namespace {
 template <int D, int NS, bool kBF16, bool kAttract, class Valid, class Gid>
 __device__ __forceinline__ void rows_steps(const BatchedArgs &a, float (&acc)[8], const float (&xi)[8],
                                            const unsigned char *rows, int row_bytes, int s0, int cnt, Valid valid,
-                                           Gid gid, int64_t voff, float lr, float &loss, int gl) {
+                                           Gid gid, int64_t voff, float lr, float &loss, bool want, int gl) {
   constexpr int LP = D / 8;
   float d[NS][8], r[NS];
   bool ok[NS];
@@ -73,7 +73,8 @@ __device__ __forceinline__ void rows_steps(const BatchedArgs &a, float (&acc)[8]
   for (int st = 0; st < NS; ++st) {
     c[st] = kAttract ? __fdividef(-2.0f, 1.0f + r[st]) : __fdividef(2.0f, (r[st] + 1e-6f) * (1.0f + r[st]));
     if (!ok[st]) c[st] = 0.f;
-    if (ok[st] && gl == 0) loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
+    if (want && ok[st] && gl == 0)
+      loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
     may_clip |= c[st] * c[st] * r[st] > 0.98f * a.bound * a.bound;
   }
   if (!__any_sync(kAll, may_clip)) {
@@ -128,6 +129,7 @@ __global__ void __launch_bounds__(512, 1) staged_rows_kernel(const BatchedArgs a
     const int skip = a.quirks ? Gi.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
     for (int e = 0; e < a.epochs; ++e) {
       const float lr = a.lr[e];
+      const bool want = a.compute_loss && e >= a.loss_from;
       double wloss = 0.0;
       for (int j = 0; j < Gi.batches; ++j) {
         const int64_t bi = Gi.batch_off + j;
@@ -229,10 +231,10 @@ __global__ void __launch_bounds__(512, 1) staged_rows_kernel(const BatchedArgs a
             int s0 = 0;
             for (; s0 + NS <= maxcnt; s0 += NS)
               rows_steps<D, NS, kBF16, true>(a, acc, xi, sub + kXiB, kRowB, s0, cnt, att_valid, att_gid, Gi.voff, lr,
-                                             loss, gl);
+                                             loss, want, gl);
             for (; s0 < maxcnt; ++s0)
               rows_steps<D, 1, kBF16, true>(a, acc, xi, sub + kXiB, kRowB, s0, cnt, att_valid, att_gid, Gi.voff, lr,
-                                            loss, gl);
+                                            loss, want, gl);
             const bool rep = has && it.part == 0 && it.row < rep_rows;
             if (__any_sync(kAll, rep) && a.ns > 0) {
               const int ncnt = rep ? a.ns : 0;
@@ -241,10 +243,10 @@ __global__ void __launch_bounds__(512, 1) staged_rows_kernel(const BatchedArgs a
               int k0 = 0;
               for (; k0 + NS <= a.ns; k0 += NS)
                 rows_steps<D, NS, kBF16, false>(a, acc, xi, negrows, kRowB, k0, ncnt, neg_ok, neg_gid, Gi.voff, lr,
-                                                loss, gl);
+                                                loss, want, gl);
               for (; k0 < a.ns; ++k0)
                 rows_steps<D, 1, kBF16, false>(a, acc, xi, negrows, kRowB, k0, ncnt, neg_ok, neg_gid, Gi.voff, lr,
-                                               loss, gl);
+                                               loss, want, gl);
             }
             if (has) {
               float *dst = it.nparts > 1 ? slots + size_t(it.first_slot + it.part) * D : stage + size_t(it.row) * D;

@@ -38,7 +38,7 @@ namespace {
 template <int D, int NS, bool kBF16, bool kAttract>
 __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8], const float (&xi)[8],
                                            const unsigned char *rows, int row_bytes, int kb, int count, unsigned vmask,
-                                           int ids, int64_t voff, float lr, float &loss, int lane) {
+                                           int ids, int64_t voff, float lr, float &loss, bool want, int lane) {
   constexpr int LP = PairLanes<D>::LP, G = PairLanes<D>::G;
   const int q = lane / LP, gl = lane % LP;
   float d[NS][8], r[NS];
@@ -91,7 +91,8 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
   for (int st = 0; st < NS; ++st) {
     c[st] = kAttract ? __fdividef(-2.0f, 1.0f + r[st]) : __fdividef(2.0f, (r[st] + 1e-6f) * (1.0f + r[st]));
     if (!ok[st]) c[st] = 0.f;
-    if (ok[st] && gl == 0) loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
+    if (want && ok[st] && gl == 0)
+      loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
     may_clip |= c[st] * c[st] * r[st] > 0.98f * a.bound * a.bound;
   }
   if (!__any_sync(kAll, may_clip)) {
@@ -111,17 +112,20 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
 template <int D, int NS, bool kBF16, bool kAttract>
 __device__ __forceinline__ void staged_pairs(const BatchedArgs &a, float (&acc)[8], const float (&xi)[8],
                                              const unsigned char *rows, int row_bytes, int count, unsigned vmask,
-                                             int ids, int64_t voff, float lr, float &loss, int lane) {
+                                             int ids, int64_t voff, float lr, float &loss, bool want, int lane) {
   constexpr int G = PairLanes<D>::G;
   int kb = 0;
   for (; kb + NS * G <= count; kb += NS * G)
-    pair_steps<D, NS, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
+    pair_steps<D, NS, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, want,
+                                       lane);
   if constexpr (NS > 1) {
     for (; kb < count; kb += G)
-      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
+      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, want,
+                                        lane);
   } else {
     if (kb < count)
-      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, lane);
+      pair_steps<D, 1, kBF16, kAttract>(a, acc, xi, rows, row_bytes, kb, count, vmask, ids, voff, lr, loss, want,
+                                        lane);
   }
 }
 
@@ -207,6 +211,7 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
     const int skip = a.quirks ? G.n - 1 : -1;  // edges into n-1 are dropped (algo.hpp:399-405, 538)
     for (int e = 0; e < a.epochs; ++e) {
       const float lr = a.lr[e];
+      const bool want = a.compute_loss && e >= a.loss_from;
       double eloss = 0.0;  // rank 0, thread 0: the epoch's loss, minibatch by minibatch
       for (int j = 0; j < G.batches; ++j) {
         const int64_t bi = G.batch_off + j;
@@ -274,10 +279,11 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
             float loss = 0.f;
             const int cnt = it.e_end - it.e_begin;
             const unsigned vmask = __ballot_sync(kAll, ids >= 0 && ids != skip);
-            staged_pairs<D, NS, kBF16, true>(a, acc, xi, slot + kXiB, kRowB, cnt, vmask, ids, G.voff, lr, loss, lane);
+            staged_pairs<D, NS, kBF16, true>(a, acc, xi, slot + kXiB, kRowB, cnt, vmask, ids, G.voff, lr, loss, want,
+                                             lane);
             if (it.part == 0 && it.row < rep_rows && a.ns > 0)
               staged_pairs<D, NS, kBF16, false>(a, acc, xi, negrows, kRowB, a.ns, neg_valid, nid, G.voff, lr, loss,
-                                                lane);
+                                                want, lane);
             // the groups' accumulators, summed; lanes of group 0 store the row
 #pragma unroll
             for (int m = 16; m >= LP; m >>= 1)
@@ -298,7 +304,7 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
         team_sync();
         combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], tw, TW, lane);
         // the minibatch's loss in item order (rank 0, warp 0), whatever team made it
-        if (a.compute_loss && trank == 0 && warp == 0) {
+        if (want && trank == 0 && warp == 0) {
           double l = 0.0;
           for (int i = lane; i < n_items; i += 32) l += double(__ldcg(item_loss + i));
 #pragma unroll

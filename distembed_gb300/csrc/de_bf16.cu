@@ -42,6 +42,14 @@ constexpr int kChunk = 64;        // negatives per GEMM chunk (one 128-B swizzle
 constexpr int kMaxKpad = 1024;    // negatives per minibatch in the BF16 form (bitmask words: 32)
 constexpr int kNearWords = kMaxKpad / 32;
 
+// 1/x by the hardware approximation (rcp.approx.ftz.f32, the reciprocal
+// __fdividef uses); 1/inf = 0.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // ------------------------------------------------------------ BF16 rows
 // Lane l holds components [l*N, l*N + N) of a row, N = dim / 32.
 
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF1
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
     if (lane == 0) {
-      a.nn[k] = sq;
+      a.nn[k] = n >= 0 ? sq : __int_as_float(0x7f800000);  // no draw: |n|^2 = +inf, so c = 0
       a.nid[k] = n;
     }
   }
@@ -517,9 +525,8 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     epi_sync();
     xx = xx_part[t] + xx_part[kTileRows + t];
 
-    float rowsum = 0.f, self_loss = 0.f;
+    float rowsum = 0.f;
     double loss = 0.0;
-    const float kSelfLoss = __logf(1.0f / 1e-6f);
     const uint32_t lane_base = uint32_t(q4 * 32) << 16;
     for (int lc = 0; lc < nloc; ++lc) {
       const int b = lc & 1;
@@ -541,43 +548,68 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       }
       tc_fence_before();
       mbar_arrive(B(S_FREE + b));
-      // Coefficients without branches, so the 32 pairs' chains interleave.
-      // Loss terms: the log of a product of eight ratios (each (1+r)/(r+1e-6)
-      // in [1, 5] for the pairs taken), summed in FP32, folded into FP64 once.
+      // Coefficients without branches, so the 32 pairs' chains interleave.  A
+      // negative that is no draw (padding, or a draw equal to n) has |n|^2 = +inf,
+      // so its r is +inf and its coefficient 0.  A pair with r < kNearR takes the
+      // exact path (bit in near_word, coefficient 0 here); that includes a row
+      // drawn as its own negative (r ~ 0), whose exact force is 0.
       uint32_t packed[16];
       uint32_t near_word = 0;  // bit i: column hf*32 + i of this chunk takes the exact path
-      float loss_c = 0.f;
+      if (!rep_active) {
 #pragma unroll
-      for (int j = 0; j < 32; j += 8) {
-        float prod = 1.f;
-        float cv[8];
+        for (int i = 0; i < 16; ++i) packed[i] = 0u;
+      } else if (a.compute_loss) {
+        // with the loss: the log of a product of eight ratios (each
+        // (1+r)/(r+1e-6) in [1, 5] for the pairs taken), summed in FP32, folded
+        // into FP64 once per chunk
+        float loss_c = 0.f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float2 m = negmeta[b][hf * 32 + j + q];
-          const int nid = __float_as_int(m.y);
-          const bool self = nid == row_global;
-          const bool valid = rep_active && nid >= 0 && !self;
-          const float r = xx + m.x - 2.0f * __uint_as_float(s_raw[j + q]);
-          const bool nearp = valid && r < kNearR;
-          const bool use = valid && !nearp;
-          // one reciprocal: q = 1/((r+1e-6)(1+r)), c = 2q, (1+r)/(r+1e-6) = (1+r)^2 q
-          const float r1 = 1.0f + r;
-          const float qr = __fdividef(1.0f, (r + 1e-6f) * r1);
-          const float cc = __bfloat162float(__float2bfloat16(2.0f * qr));
-          cv[q] = use ? cc : 0.f;
-          prod *= use ? r1 * r1 * qr : 1.0f;
-          self_loss += (rep_active && self) ? kSelfLoss : 0.f;
-          near_word |= nearp ? (1u << (j + q)) : 0u;
-          rowsum += cv[q];
+        for (int j = 0; j < 32; j += 8) {
+          float prod = 1.f;
+          float cv[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float2 m = negmeta[b][hf * 32 + j + q];
+            const float r = xx + m.x - 2.0f * __uint_as_float(s_raw[j + q]);
+            const bool nearp = r < kNearR;
+            // one reciprocal: q = 1/((r+1e-6)(1+r)), c = 2q, (1+r)/(r+1e-6) = (1+r)^2 q
+            const float r1 = 1.0f + r;
+            const float qr = rcp_approx((r + 1e-6f) * r1);
+            const float cc = __bfloat162float(__float2bfloat16(2.0f * qr));
+            cv[q] = nearp ? 0.f : cc;
+            prod *= (nearp || qr == 0.f) ? 1.0f : r1 * r1 * qr;
+            near_word |= nearp ? (1u << (j + q)) : 0u;
+            rowsum += cv[q];
+          }
+#pragma unroll
+          for (int q = 0; q < 8; q += 2) {
+            __nv_bfloat162 p2 = __floats2bfloat162_rn(cv[q], cv[q + 1]);
+            packed[(j + q) / 2] = *reinterpret_cast<uint32_t *>(&p2);
+          }
+          loss_c += __logf(prod);
         }
+        loss += double(loss_c);
+      } else {
+        // no loss: two pairs per packed f32x2 instruction; the row sum adds the
+        // BF16-rounded coefficients the second GEMM multiplies with
+        const float2 xx2 = make_float2(xx, xx);
+        float2 rs2 = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int q = 0; q < 8; q += 2) {
-          __nv_bfloat162 p2 = __floats2bfloat162_rn(cv[q], cv[q + 1]);
-          packed[(j + q) / 2] = *reinterpret_cast<uint32_t *>(&p2);
+        for (int j = 0; j < 32; j += 2) {
+          const float4 m = *reinterpret_cast<const float4 *>(&negmeta[b][hf * 32 + j]);  // (nn, id) x 2
+          const float2 s2 = make_float2(__uint_as_float(s_raw[j]), __uint_as_float(s_raw[j + 1]));
+          const float2 r2 = __ffma2_rn(make_float2(-2.f, -2.f), s2, __fadd2_rn(xx2, make_float2(m.x, m.z)));
+          const float2 den = __fmul2_rn(__fadd2_rn(r2, make_float2(1e-6f, 1e-6f)), __fadd2_rn(r2, make_float2(1.f, 1.f)));
+          const bool n0 = r2.x < kNearR, n1 = r2.y < kNearR;
+          const float2 c2 = __fmul2_rn(make_float2(2.f, 2.f), make_float2(rcp_approx(den.x), rcp_approx(den.y)));
+          __nv_bfloat162 p2 = __floats2bfloat162_rn(n0 ? 0.f : c2.x, n1 ? 0.f : c2.y);
+          const uint32_t pw = *reinterpret_cast<uint32_t *>(&p2);
+          packed[j / 2] = pw;
+          near_word |= (n0 ? (1u << j) : 0u) | (n1 ? (2u << j) : 0u);
+          rs2 = __fadd2_rn(rs2, make_float2(__uint_as_float(pw << 16), __uint_as_float(pw & 0xffff0000u)));
         }
-        loss_c += __logf(prod);
+        rowsum += rs2.x + rs2.y;
       }
-      loss += double(loss_c);
       if (near_word) near_loc[lc * 2] = near_word;
       if (lc >= 2) mbar_wait(B(C_FREE + b), ((lc >> 1) + 1) & 1, &err);
       unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
@@ -593,7 +625,6 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const bool done = __all_sync(kFull, mbar_wait(B(F_DONE), 0, &err) && !failed());
     tc_fence_after();
     // combine the two column halves of each row
-    loss += double(self_loss);
     float *rs_part = reinterpret_cast<float *>(sC_ptr[0]);
     double *loss_part = reinterpret_cast<double *>(sC_ptr[0] + 1024);
     rs_part[hf * kTileRows + t] = rowsum;

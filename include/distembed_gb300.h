@@ -222,6 +222,14 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
  * this off.  Close pairs are the ones whose distance the BF16 rounding step
  * distorts. */
 int de_batch_set_near_distance(de_batch *b, float near_r);
+/* Which epochs of a run compute their FP64 loss (the reference computes none):
+ * DE_LOSS_EVERY_EPOCH (default), DE_LOSS_LAST_EPOCH (only the last epoch of each
+ * run; the others report 0, and their passes take no logarithm) or DE_LOSS_NONE.
+ * Takes effect at the next de_batch_prepare / de_batch_run. */
+#define DE_LOSS_NONE 0
+#define DE_LOSS_EVERY_EPOCH 1
+#define DE_LOSS_LAST_EPOCH 2
+int de_batch_set_loss(de_batch *b, int32_t mode);
 /* Per graph of the last launch: {start, end} (globaltimer ns) and the team that
  * ran it; out holds n_graphs x 3 values.  Waits for the stream. */
 int de_batch_trace(de_batch *b, int64_t *out);

@@ -82,6 +82,39 @@ def _load(name):
     return L
 
 
+_GPU = None
+
+
+def lib_gpu():
+    """The FP64 GPU restatement (liboracle_gpu.so, built by `make -C oracle gpu`)."""
+    global _GPU
+    if _GPU is None:
+        path = os.path.join(HERE, "liboracle_gpu.so")
+        src = os.path.join(HERE, "de_oracle_gpu.cu")
+        if not os.path.exists(path) or os.path.getmtime(src) > os.path.getmtime(path):
+            subprocess.check_call(["make", "-s", "-C", HERE, "gpu"])
+        L = ctypes.CDLL(path)
+        L.oracle_gpu_run.argtypes = [ctypes.c_int64, _i64p, _i64p, ctypes.c_int, _f64p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, _f64p, ctypes.c_int, _f64p, ctypes.c_int]
+        _GPU = L
+    return _GPU
+
+
+def gpu_run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, device=0):
+    """oracle.run on the GPU in FP64 (the same arithmetic in the same order, so
+    the embedding is bitwise oracle.run's): returns (x_new, loss_per_epoch)."""
+    rowptr, col = _csr(rowptr, col)
+    x = np.array(x, dtype=np.float64, order="C", copy=True)
+    n, dim = x.shape
+    lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
+    loss = np.zeros(max(epochs, 1), dtype=np.float64)
+    rc = lib_gpu().oracle_gpu_run(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epochs, batch, ns,
+                                  _p(lrs, _f64p), int(quirks), _p(loss, _f64p), device)
+    if rc != 0:
+        raise ValueError(f"oracle_gpu_run failed ({rc})")
+    return x, loss[:epochs]
+
+
 def ref_path() -> str:
     return os.path.join(HERE, "_ref", "libderef.so")
 
