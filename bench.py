@@ -30,7 +30,8 @@ FP32 plain form on one GB300, final loss against the FP64 oracle, job p50/p99):
 --impl reference times the reference's CPU algorithm (the FP64 port in oracle/,
 -O3, every host core, one graph per thread) on the same 512 graphs; one step is
 one epoch of every graph.  --form plain|bf16|batched|served|spmm|sparse prints the
-line of one form alone (plain: R-MAT scale 20; bf16: R-MAT scale 22, dim 256, 1024
+line of one form alone (plain: R-MAT scale 20; knn20k: the CPU-runnable 20,000-point kNN
+workload; bf16: R-MAT scale 22, dim 256, 1024
 shared negatives; batched: the default workload without the other forms; served:
 the arrival stream; spmm and sparse: the "next" steps on R-MAT scale 20).
 
@@ -72,8 +73,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="plain form: overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="plain form: max CSR entries per work item (0: automatic)")
+    p.add_argument("--stage-negs", type=int, default=0,
+                   help="plain form: 1 copies the negative rows into shared memory (bulk copies) per CTA")
     p.add_argument("--form", default="headline",
-                   choices=["headline", "plain", "bf16", "batched", "served", "spmm", "sparse"],
+                   choices=["headline", "plain", "knn20k", "bf16", "batched", "served", "spmm", "sparse"],
                    help="headline (default): the metric's comparison on the batched workload with every other "
                         "form beside it; the others print one form alone")
     p.add_argument("--graphs", type=int, default=512, help="batched workload: number of graphs")
@@ -227,7 +230,7 @@ def plain_leg(args, rank, world, local, with_cpu, with_gap):
             torch.distributed.barrier()
 
     h = de.Handle(rowptr, col, dim, device=local, quirks=True, compute_loss=True, pdl=bool(args.pdl),
-                  edge_cap=args.edge_cap)
+                  edge_cap=args.edge_cap, stage_negatives=bool(args.stage_negs))
     stream = torch.cuda.ExternalStream(h.stream, device=local)
     h.set_embeddings(x0)
     upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
@@ -324,7 +327,7 @@ def plain_leg(args, rank, world, local, with_cpu, with_gap):
                    "lr": lr, "epochs_per_job": E, "step": "one epoch (256 minibatches, CUDA graph)",
                    "l2": "inputs larger than L2 (512 MiB FP32 embedding); no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU", "ref_quirks": True,
-                   "pdl": bool(args.pdl), "edge_cap": args.edge_cap},
+                   "pdl": bool(args.pdl), "edge_cap": args.edge_cap, "stage_negatives": bool(args.stage_negs)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "kernel": "plain_batch_kernel<128>",
@@ -353,6 +356,123 @@ def run_plain_form(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+W1 = dict(n=20000, pts_dim=64, k=15, components=10, seed=0, dim=128, batch=256, ns=5, lr=0.02, epochs=30, init_seed=0)
+
+
+def l2_copy_peak(device=0):
+    """Copy bandwidth of a buffer that stays in L2 (8 MiB read + 8 MiB written,
+    best of 50 CUDA-event-timed copies): the measured L2-side peak."""
+    import torch
+    a = torch.empty(2 << 20, dtype=torch.float32, device=device)
+    b = torch.empty_like(a)
+    best = None
+    for _ in range(60):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1)
+        best = t if best is None else min(best, t)
+    return 2 * a.numel() * 4 / (best / 1e3) / 1e9
+
+
+def run_knn20k_form(args):
+    """The CPU-runnable workload on the GPU: 20,000-point 64-D Gaussian-mixture kNN
+    graph (k=15, symmetrised), dim 128, minibatch 256, 5 negatives, lr 0.02 decayed
+    linearly over 30 epochs.  One step = one epoch (79 minibatches, CUDA graph).
+    The embedding (10 MB) stays in L2, so the step is latency-bound, not HBM-bound."""
+    import torch
+
+    import distembed_gb300 as de
+    import oracle
+    from distembed_gb300 import graphgen as gg
+    torch.cuda.set_device(0)
+    n, rowptr, col = gg.knn_csr(W1["n"], W1["pts_dim"], W1["k"], W1["components"], seed=W1["seed"])
+    x0 = gg.init_embedding(n, W1["dim"], seed=W1["init_seed"]).astype(np.float32).astype(np.float64)
+    dim, B, ns, E = W1["dim"], W1["batch"], W1["ns"], W1["epochs"]
+    lrs = [W1["lr"] * (1 - e / E) for e in range(E)]
+    batches = (n + B - 1) // B
+    h = de.Handle(rowptr, col, dim, quirks=True, compute_loss=False, pdl=bool(args.pdl))
+    stream = torch.cuda.ExternalStream(h.stream, device=0)
+    h.set_embeddings(x0)
+    upd = [h.edge_updates(1, B, ns, first_epoch=e) for e in range(E)]
+    for k in range(args.warmup):
+        h.run(1, B, ns, lrs[k % E], want_loss=False, first_epoch=k % E)
+    h.sync()
+    clocks = Clocks(0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev[0].record(stream)
+    for k in range(args.steps):
+        h.run(1, B, ns, lrs[k % E], want_loss=False, first_epoch=k % E)
+        ev[k + 1].record(stream)
+    h.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    value = sum(upd[k % E] for k in range(args.steps)) / (sum(step_ms) / 1e3)
+    nnz_eff = len(col) - int(np.sum(col == n - 1))
+    alg = algorithmic_bytes_per_epoch(n, nnz_eff, batches, dim, ns)
+    achieved = alg / (statistics.mean(step_ms) / 1e3) / 1e9
+    l2 = l2_copy_peak(0)
+    pms, kind = h.profile_epoch(B, ns, lrs[0], first_epoch=0)
+    launch_us = float(pms[kind == 0].mean()) * 1e3
+    # end to end: the reference-facing call, host FP64 in, the 30-epoch job, host FP64 out
+    x_host = torch.empty((n, dim), dtype=torch.float64, pin_memory=True).numpy()
+    x_host[:] = x0
+    out_host = torch.empty((n, dim), dtype=torch.float64, pin_memory=True).numpy()
+    ts = []
+    for k in range(max(args.e2e_steps, 1) + 1):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        h.set_embeddings(x_host)
+        h.run(E, B, ns, lrs, want_loss=False)
+        h.get_embeddings(out=out_host)
+        if k > 0:
+            ts.append(time.perf_counter() - t1)
+    h.close()
+    e2e = {"value": sum(upd) / statistics.mean(ts), "unit": UNIT, "h2d_bytes_per_step": n * dim * 8 + E * batches * ns * 4,
+           "d2h_bytes_per_step": n * dim * 8, "ms_per_step": 1e3 * statistics.mean(ts),
+           "step": "EmbeddingAlgo call: host FP64 x in (pinned), 30 epochs, host FP64 x out"}
+    # the whole job against the FP64 oracle, and the CPU baseline on the same job
+    with de.Handle(rowptr, col, dim, quirks=True) as hl:
+        hl.set_embeddings(x0)
+        lg = hl.run(E, B, ns, lrs)
+        xg = hl.get_embeddings()
+    threads = os.cpu_count() or 1
+    xo, lo = oracle.run(rowptr, col, x0, E, B, ns, lrs, quirks=True, threads=threads)
+    t1 = time.perf_counter()
+    oracle.run(rowptr, col, x0, E, B, ns, lrs, quirks=True, threads=threads, want_loss=False, fast=True)
+    cs = time.perf_counter() - t1
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic: 20,000 points of a 10-component 64-D Gaussian mixture (seed 0, means ~N(0,4I)), exact "
+                    "kNN k=15 symmetrised; U[-0.5,0.5] init (seed 0)",
+            "config": {"workload": "knn20k_d128_b256_ns5_e30_fp32_plain", "n": n, "nnz": int(len(col)), "dim": dim,
+                       "batch": B, "ns": ns, "lr": "0.02 (1 - e/30)", "epochs_per_job": E,
+                       "step": f"one epoch ({batches} minibatches, CUDA graph)",
+                       "l2": "L2-resident (10 MB FP32 embedding): latency-bound; no flush"},
+            "roofline": {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
+                         "peak_source": "measured here: L2-resident copy (8 MiB), best of 60",
+                         "kernel": "plain_batch_kernel<128>", "algorithmic_bytes_per_epoch": alg,
+                         "launch_us_serial": launch_us, "launches_per_epoch": batches + 1,
+                         "note": "79 dependent minibatch launches per epoch of 256 rows each: one launch is a few "
+                                 "microseconds of work, so launch latency and the minibatch chain bound it"},
+            "cpu_baseline": {"value": sum(upd) / cs, "unit": UNIT, "cores": threads, "kind": "port",
+                             "build": "g++ -O3 -ffp-contract=fast -fopenmp (oracle/liboracle_fast.so)",
+                             "sample": f"the whole 30-epoch job, FP64, OpenMP over the rows of a minibatch, {cs:.2f} s"},
+            "e2e": e2e,
+            "gap_vs_fp64_oracle": {"loss_rel_max": float(np.max(np.abs(lg - lo) / lo)),
+                                   "final_loss_rel": float(abs(lg[-1] - lo[-1]) / lo[-1]),
+                                   "x_rel_l2_final": float(np.linalg.norm(xg - xo) / np.linalg.norm(xo))},
+            "gpu_launches": args.steps * (batches + 1), "clocks": clk}
+    print(json.dumps(line), flush=True)
 
 
 W3 = dict(scale=22, edge_factor=16, seed=2, dim=256, batch=8192, ns=1024, lr=0.02, epochs=10, init_seed=0)
@@ -1307,6 +1427,8 @@ def main():
         run_reference(args)
     elif args.form == "plain":
         run_plain_form(args)
+    elif args.form == "knn20k":
+        run_knn20k_form(args)
     elif args.form == "bf16":
         run_bf16_form(args)
     elif args.form == "batched":

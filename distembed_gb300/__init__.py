@@ -92,7 +92,8 @@ class DEError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("ref_quirks", ctypes.c_int32), ("compute_loss", ctypes.c_int32),
                 ("device", ctypes.c_int32), ("stream", ctypes.c_void_p), ("max_bound", ctypes.c_double),
-                ("edge_cap", ctypes.c_int32), ("pdl", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("edge_cap", ctypes.c_int32), ("pdl", ctypes.c_int32), ("stage_negatives", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 _lib = None
@@ -256,7 +257,7 @@ class Handle:
 
     def __init__(self, rowptr, col, dim: int, precision: str = "fp32", quirks: bool = True,
                  compute_loss: bool = True, device: int = 0, stream: int | None = None,
-                 max_bound: float = 5.0, edge_cap: int = 0, pdl: bool = True):
+                 max_bound: float = 5.0, edge_cap: int = 0, pdl: bool = True, stage_negatives: bool = False):
         L = lib()
         self._rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
         self._col = np.ascontiguousarray(col, dtype=np.int64)
@@ -273,6 +274,7 @@ class Handle:
         o.max_bound = max_bound
         o.edge_cap = edge_cap
         o.pdl = int(pdl)
+        o.stage_negatives = int(stage_negatives)
         h = _vp()
         rc = L.de_create(self.n, self._rowptr.ctypes.data, self._col.ctypes.data if self.nnz else None, self.nnz,
                          dim, ctypes.byref(o), ctypes.byref(h))

@@ -76,7 +76,12 @@ struct PlainBatchArgs {
   double *loss_partial;     // one per work item of the epoch
   int64_t loss_off;         // first item of this minibatch in the epoch
   const int32_t *epoch;     // device [2]: epoch index within this call, first epoch of the call
+  int32_t stage_negs;       // 1: the minibatch's final negative rows are copied into every CTA's
+                            // shared memory (cp.async.bulk) before the repulsive pass; ns <= kStageNegMax
+  int32_t *err;             // set when a bounded device wait gives up
 };
+
+constexpr int kStageNegMax = 8;  // negatives per minibatch the shared-memory staging takes
 
 struct FlushArgs {
   float *X;

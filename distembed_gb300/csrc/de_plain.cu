@@ -25,6 +25,7 @@
 // in flight and launch j+1's early phase only ever reads rows that are final.
 #include <cuda_runtime.h>
 
+#include "de_async.cuh"
 #include "de_device.cuh"
 #include "de_internal.h"
 
@@ -82,9 +83,51 @@ __device__ __forceinline__ void force_lanes(const PlainBatchArgs &a, Frag<D> &ac
   if (k < cnt) force_group<D, U / 2, kAttract, kAfterWait>(a, acc, xi, ids, k, lr, bound, want_loss, loss, lane);
 }
 
+// A row held in shared memory, in the Frag layout.
+template <int D>
+__device__ __forceinline__ void load_smem(Frag<D> &f, const float *row, int lane) {
+  if constexpr (D == 32) {
+    f.v[0] = row[lane];
+  } else if constexpr (D == 64) {
+    const float2 t = reinterpret_cast<const float2 *>(row)[lane];
+    f.v[0] = t.x; f.v[1] = t.y;
+  } else {
+    const float4 t = reinterpret_cast<const float4 *>(row)[lane];
+    f.v[0] = t.x; f.v[1] = t.y; f.v[2] = t.z; f.v[3] = t.w;
+    if constexpr (D == 256) {
+      const float4 u = reinterpret_cast<const float4 *>(row)[32 + lane];
+      f.v[4] = u.x; f.v[5] = u.y; f.v[6] = u.z; f.v[7] = u.w;
+    }
+  }
+}
+
+// Repulsive forces of staged negatives k0 .. k0+V-1 (rows in shared memory;
+// draws whose bit in `staged` is clear are left out).
+template <int D, int V>
+__device__ __forceinline__ void staged_group(Frag<D> &acc, const Frag<D> &xi, const float *negsm, unsigned staged,
+                                             int k0, int ns, float lr, float bound, bool want_loss, float &loss,
+                                             int lane) {
+  Frag<D> xn[V];
+  unsigned mask = 0;
+#pragma unroll
+  for (int u = 0; u < V; ++u) {
+    const int k = k0 + u;
+    if (k < ns && ((staged >> k) & 1u)) {
+      load_smem(xn[u], negsm + k * D, lane);
+      mask |= 1u << u;
+    } else {
+      xn[u] = xi;
+    }
+  }
+  if (mask) pair_forces<D, V, false>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
+}
+
 template <int D, int U>
 __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBlocks)
     plain_batch_kernel(const PlainBatchArgs a) {
+  extern __shared__ __align__(16) float negsm[];  // stage_negs: [ns, D] rows of the minibatch's draws
+  __shared__ __align__(8) uint64_t negbar;
+  __shared__ int negerr;
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * kPlainWarps + (threadIdx.x >> 5);
   const int total_w = gridDim.x * kPlainWarps;
@@ -110,6 +153,32 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
   const bool repulse = has_item && it.part == 0 && it.row < rep_rows;
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
 
+  // Staged negatives: bit k of `staged`: draw k is a vertex outside minibatch j-1
+  // (final before the wait), copied by one thread of the CTA into row k of negsm
+  // with bulk asynchronous copies; the CTA waits (bounded) on one barrier.
+  unsigned staged = 0;
+  if (a.stage_negs) {
+    for (int k = 0; k < a.ns; ++k) {
+      const int nid = __ldg(negs + k);
+      if (nid >= 0 && nid < a.n && !in_prev(a, nid)) staged |= 1u << k;
+    }
+    const uint32_t bar = smem_u32(&negbar);
+    if (threadIdx.x == 0) {
+      negerr = 0;
+      mbar_init(bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      mbar_expect_tx(bar, uint32_t(__popc(staged)) * D * 4u);
+      for (int k = 0; k < a.ns; ++k)
+        if ((staged >> k) & 1u)
+          bulk_g2s(smem_u32(negsm + k * D), row_ptr<false>(a, __ldg(negs + k), D), D * 4u, bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(bar, 0, &negerr)) {
+      if (lane == 0) atomicExch(a.err, 1);
+      staged = 0;  // results of this launch are invalid; the host reports the error
+    }
+  }
+
   float loss = 0.f;  // this item's loss terms (FP32); the epoch sum is FP64
   Frag<D> xi, acc;
   acc.zero();
@@ -117,7 +186,14 @@ __global__ void __launch_bounds__(kPlainWarps * 32, D >= 256 ? 4 : kPlainMinBloc
     load_nc(xi, a.X + size_t(a.base + it.row) * D, lane);
     // ---- before the wait: forces whose other row is final (CSR order, then draw order)
     force_lanes<D, U, true, false>(a, acc, xi, defer ? -1 : ids, cnt, lr, bound, want_loss, loss, lane);
-    if (repulse)
+    if (repulse && a.stage_negs) {
+      // the staged rows in draw order, grouped as force_lanes groups them (so the
+      // arithmetic, and the result, equal the unstaged path's)
+      int k0 = 0;
+      for (; k0 + U / 2 < a.ns; k0 += U)
+        staged_group<D, U>(acc, xi, negsm, staged, k0, a.ns, lr, bound, want_loss, loss, lane);
+      if (k0 < a.ns) staged_group<D, U / 2>(acc, xi, negsm, staged, k0, a.ns, lr, bound, want_loss, loss, lane);
+    } else if (repulse)
       for (int k0 = 0; k0 < a.ns; k0 += 32) {
         const int kc = min(32, a.ns - k0);
         int nid = lane < kc ? __ldg(negs + k0 + lane) : -1;
@@ -305,11 +381,11 @@ __global__ void f32_to_f64_kernel(const float *__restrict__ s, double *__restric
 }
 
 template <typename Args>
-cudaError_t launch(void (*k)(Args), int grid, int block, const Args &a, bool pdl, cudaStream_t s) {
+cudaError_t launch(void (*k)(Args), int grid, int block, const Args &a, bool pdl, cudaStream_t s, size_t smem = 0) {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -323,11 +399,13 @@ cudaError_t launch(void (*k)(Args), int grid, int block, const Args &a, bool pdl
 
 cudaError_t launch_plain_batch(int dim, const PlainBatchArgs &a, int grid, bool pdl, cudaStream_t s) {
   const int block = kPlainWarps * 32;
+  if (a.stage_negs && a.ns > kStageNegMax) return cudaErrorInvalidValue;
+  const size_t smem = a.stage_negs ? size_t(a.ns) * dim * sizeof(float) : 0;
   switch (dim) {
-    case 32: return launch(plain_batch_kernel<32, 8>, grid, block, a, pdl, s);
-    case 64: return launch(plain_batch_kernel<64, 8>, grid, block, a, pdl, s);
-    case 128: return launch(plain_batch_kernel<128, 8>, grid, block, a, pdl, s);
-    case 256: return launch(plain_batch_kernel<256, 4>, grid, block, a, pdl, s);
+    case 32: return launch(plain_batch_kernel<32, 8>, grid, block, a, pdl, s, smem);
+    case 64: return launch(plain_batch_kernel<64, 8>, grid, block, a, pdl, s, smem);
+    case 128: return launch(plain_batch_kernel<128, 8>, grid, block, a, pdl, s, smem);
+    case 256: return launch(plain_batch_kernel<256, 4>, grid, block, a, pdl, s, smem);
     default: return cudaErrorInvalidValue;
   }
 }

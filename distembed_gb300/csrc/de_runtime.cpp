@@ -451,6 +451,8 @@ cudaError_t enqueue_epoch_plain(de_handle *h, int ns, cudaStream_t st, cudaEvent
     a.loss_partial = h->d_loss_partial;
     a.loss_off = s.item_off[j];
     a.epoch = h->d_epoch;
+    a.stage_negs = h->opt.stage_negatives && ns > 0 && ns <= kStageNegMax;
+    a.err = h->d_err;
     const int grid = int(s.cta_off[j + 1] - s.cta_off[j]);
     if (ev) cudaEventRecord(ev[j], st);
     err = launch_plain_batch(h->dim, a, grid, h->opt.pdl && j > 0 && !ev, st);

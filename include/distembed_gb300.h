@@ -55,7 +55,10 @@ typedef struct de_options {
   int32_t edge_cap;     /* max CSR entries per work item (1..32); 0 = automatic        */
   int32_t pdl;          /* 1: overlap consecutive minibatch launches (programmatic     */
                         /*    dependent launch); 0: plain stream order                 */
-  int32_t reserved[6];
+  int32_t stage_negatives; /* FP32 plain form, ns <= 8: 1 copies the minibatch's      */
+                        /*    negative rows into each CTA's shared memory (bulk async  */
+                        /*    copy) before the repulsive pass; 0 reads them from L1/L2 */
+  int32_t reserved[5];
 } de_options;
 
 /* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5,

@@ -175,18 +175,19 @@ def batch_grad(rowptr, col, x, batch, ns, lr, batch_id, seed, rep, quirks=True):
     return prev, rl
 
 
-def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0):
-    """Runs `epochs` epochs; returns (x_new, loss_per_epoch).  lr: scalar or per-epoch array."""
+def run(rowptr, col, x, epochs, batch, ns, lr, quirks=True, threads=0, want_loss=True, fast=False):
+    """Runs `epochs` epochs; returns (x_new, loss_per_epoch or None).  lr: scalar or
+    per-epoch array.  fast: the -O3 build (the timed CPU baseline)."""
     rowptr, col = _csr(rowptr, col)
     x = np.array(x, dtype=np.float64, order="C", copy=True)
     n, dim = x.shape
     lrs = np.ascontiguousarray(np.broadcast_to(np.asarray(lr, dtype=np.float64), (max(epochs, 1),)))
-    loss = np.zeros(max(epochs, 1), dtype=np.float64)
-    rc = lib().oracle_run(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epochs, batch, ns,
-                          _p(lrs, _f64p), int(quirks), _p(loss, _f64p), threads)
+    loss = np.zeros(max(epochs, 1), dtype=np.float64) if want_loss else None
+    rc = (lib_fast() if fast else lib()).oracle_run(n, _p(rowptr, _i64p), _p(col, _i64p), dim, _p(x, _f64p), epochs,
+                                                    batch, ns, _p(lrs, _f64p), int(quirks), _p(loss, _f64p), threads)
     if rc != 0:
         raise ValueError(f"oracle_run failed ({rc})")
-    return x, loss[:epochs]
+    return x, (loss[:epochs] if want_loss else None)
 
 
 def run_many(graphs, xs, epochs, batch, ns, lr, first_epoch=0, quirks=True, want_loss=True, threads=0,

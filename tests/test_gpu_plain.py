@@ -250,3 +250,18 @@ def test_reference_interface_updates_in_place():
     loss = algo.algo_force2_vec_ns(2, 64, 5, 0.02)
     assert loss.shape == (2,)
     assert rel_l2(dense, want) <= RUN_REL_L2
+
+
+@pytest.mark.parametrize("dim,ns", [(32, 5), (64, 8), (128, 5), (256, 7)])
+def test_staged_negatives_bitwise_equal(dim, ns):
+    # negatives copied into shared memory (bulk asynchronous copies) or read from
+    # L1/L2: the same pairs in the same order, so the same bits
+    n, rp, col = gg.rmat_csr(12, 8, seed=27)
+    x0 = f32(gg.init_embedding(n, dim, seed=15))
+    out = []
+    for stage in (False, True):
+        with de.Handle(rp, col, dim, stage_negatives=stage, edge_cap=16) as h:
+            h.set_embeddings(x0)
+            loss = h.run(3, 300, ns, 0.03)
+            out.append((h.get_embeddings(), loss))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
