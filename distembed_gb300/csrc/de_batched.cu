@@ -56,8 +56,10 @@ struct KernelPick {
 
 KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) {
   KernelPick k;
-  if (s.team_ctas > 2 || (s.team_ctas == 2 && s.kernel != DE_BATCH_STAGED)) return k;
-  k.ctas = s.team_ctas == 2 ? 2 : 1;
+  if ((s.team_ctas > 1 && s.team_ctas != 2 && s.team_ctas != 4) ||
+      (s.team_ctas > 1 && s.kernel != DE_BATCH_STAGED))
+    return k;
+  k.ctas = s.team_ctas > 1 ? s.team_ctas : 1;
   if (s.kernel == DE_BATCH_REGISTER) {
     if (s.edge_cap < 1 || s.edge_cap > 4096) return k;
     k.fn = pick_register(dim, bf16, s.vertices_per_warp, s.team_warps);
@@ -275,14 +277,14 @@ int teams_for(de_batch *b, const KernelPick &k) {
     per_sm = 1;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms < 1) sms = 1;
   if (k.ctas == 1) return std::min(per_sm * sms, b->n_graphs);
-  // clusters of two CTAs: as many as can be resident at once (a cluster sits in one GPC)
+  // clusters of k.ctas CTAs: as many as can be resident at once (a cluster sits in one GPC)
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(2 * per_sm * sms);
+  cfg.gridDim = dim3(k.ctas * per_sm * sms);
   cfg.blockDim = dim3(k.block);
   cfg.dynamicSmemBytes = k.smem;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.x = k.ctas;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -290,9 +292,9 @@ int teams_for(de_batch *b, const KernelPick &k) {
   int clusters = 0;
   if (cudaOccupancyMaxActiveClusters(&clusters, k.fn, &cfg) != cudaSuccess || clusters < 1) {
     cudaGetLastError();
-    clusters = std::max(1, per_sm * sms / 2);
+    clusters = std::max(1, per_sm * sms / k.ctas);
   }
-  return 2 * std::min(clusters, (b->n_graphs + 1) / 2);
+  return k.ctas * std::min(clusters, (b->n_graphs + k.ctas - 1) / k.ctas);
 }
 
 // Everything of a run except the launch: schedule, negatives, rates, team staging
@@ -339,7 +341,8 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   if (int rc = bgrow(b, &b->d_stage, &b->stage_cap, size_t(teams) * B * b->dim)) return rc;
   if (int rc = bgrow(b, &b->d_slots, &b->slots_cap, size_t(teams) * b->max_slots * b->dim)) return rc;
   if (int rc = bgrow(b, &b->d_item_loss, &b->item_loss_cap, size_t(teams) * b->max_batch_items)) return rc;
-  if (int rc = bgrow(b, &b->d_cluster_slot, &b->cluster_slot_cap, size_t(teams / 2 + 1))) return rc;
+  if (int rc = bgrow(b, &b->d_cluster_slot, &b->cluster_slot_cap, size_t(teams / std::max(k.ctas, 1) + 1)))
+    return rc;
   // graphs largest first by work (CSR entries, repulsive pairs and a fixed cost per
   // minibatch, all per epoch); with two-CTA teams the graphs above 0.6 of the
   // balanced share of one CTA are trained by a whole cluster
@@ -352,7 +355,7 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
     }
     std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return w[x] > w[y]; });
     b->n_big = 0;
-    if (k.ctas == 2)
+    if (k.ctas > 1)
       while (b->n_big < b->n_graphs && w[b->order[b->n_big]] > 0.6 * total_w / teams) ++b->n_big;
     BCUDA(b, cudaMemcpyAsync(b->d_order, b->order.data(), b->order.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                              b->stream));
@@ -414,7 +417,7 @@ int launch_batched(de_batch *b, cudaStream_t st) {
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.x = b->ctas;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -686,10 +689,11 @@ int de_batch_autotune(de_batch *b, int32_t epochs, int32_t batch_size, int32_t n
         for (int c : {8, 16, 32})
           for (int u : {1, 2})
             for (int st : {3, 4}) cand.push_back(de_batch_shape{fam, 0, w, c, u, st, 1});
-    for (int w : {8, 16})
-      for (int c : {16, 32})
-        for (int u : {1, 2})
-          for (int st : {3, 4}) cand.push_back(de_batch_shape{DE_BATCH_STAGED, 0, w, c, u, st, 2});
+    for (int ct : {2, 4})
+      for (int w : {8, 16})
+        for (int c : {16, 32})
+          for (int u : {1, 2})
+            for (int st : {3, 4}) cand.push_back(de_batch_shape{DE_BATCH_STAGED, 0, w, c, u, st, ct});
   }
   const bool bf16 = b->opt.precision == DE_PRECISION_BF16;
   std::vector<double> lrs(epochs, lr);

@@ -136,16 +136,16 @@ __device__ __forceinline__ int cluster_rank() {
   return r;
 }
 
-// Both CTAs of the cluster: every thread arrives (release) and waits (acquire),
-// so each CTA's global writes before the barrier are visible to the other after it.
+// Every CTA of the cluster: every thread arrives (release) and waits (acquire),
+// so each CTA's global writes before the barrier are visible to the others after it.
 __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// A team is one CTA or, with CT = 2, the two CTAs of a cluster working on one
+// A team is one CTA or, with CT = 2 or 4, the CTAs of a cluster working on one
 // graph: team warp tw = rank * W + warp of TW = nct * W, one shared staging area
-// (that of rank 0), barriers across both CTAs.  With CT = 2 a cluster first takes
-// the big graphs (order[0, n_big)) as one team; when they are gone its CTAs
+// (that of rank 0), barriers across the cluster.  With CT > 1 a cluster first
+// takes the big graphs (order[0, n_big)) as one team; when they are gone its CTAs
 // take the remaining graphs one each.  The loss of an epoch is summed from the
 // per-item losses in item order, so it does not depend on the team's make-up.
 template <int D, int NS, int S, bool kBF16, int CT>
@@ -165,20 +165,20 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
   const unsigned char *src = kBF16 ? reinterpret_cast<const unsigned char *>(a.xb)
                                    : reinterpret_cast<const unsigned char *>(a.xm);
   const unsigned char *srcm = reinterpret_cast<const unsigned char *>(a.xm);
-  const int rank = CT == 2 ? cluster_rank() : 0;
-  bool coop = CT == 2;
+  const int rank = CT > 1 ? cluster_rank() : 0;
+  bool coop = CT > 1;
 
   for (;;) {
     int g;
     if (coop) {
       if (threadIdx.x == 0 && rank == 0) {
         const int i = atomicAdd(a.next_big, 1);
-        *reinterpret_cast<volatile int *>(a.cluster_slot + blockIdx.x / 2) = i < a.n_big ? a.order[i] : -1;
+        *reinterpret_cast<volatile int *>(a.cluster_slot + blockIdx.x / CT) = i < a.n_big ? a.order[i] : -1;
         __threadfence();
       }
       cluster_sync();
-      g = __ldcg(a.cluster_slot + blockIdx.x / 2);
-      cluster_sync();  // rank 0 rewrites the slot only after both have read it
+      g = __ldcg(a.cluster_slot + blockIdx.x / CT);
+      cluster_sync();  // rank 0 rewrites the slot only after every rank has read it
       if (g < 0) {
         coop = false;
         continue;
@@ -193,14 +193,14 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
       __syncthreads();
       if (g < 0) break;
     }
-    const int nct = coop ? 2 : 1, trank = coop ? rank : 0;
+    const int nct = coop ? CT : 1, trank = coop ? rank : 0;
     const int tw = trank * W + warp, TW = nct * W;
     const int team_blk = blockIdx.x - trank;
     float *stage = a.stage + size_t(team_blk) * a.batch * D;
     float *slots = a.slots + size_t(team_blk) * a.slot_stride * D;
     float *item_loss = a.item_loss + size_t(team_blk) * a.item_stride;
     auto team_sync = [&]() {
-      if (nct == 2) cluster_sync();
+      if (nct > 1) cluster_sync();
       else __syncthreads();
     };
     if (a.trace && threadIdx.x == 0 && trank == 0) {
@@ -335,6 +335,7 @@ template <int D, bool kBF16>
 BatchedKernel pick_staged_fn(int steps, int stages, int ctas) {
   if (ctas == 1) return pick_staged_ct<D, kBF16, 1>(steps, stages);
   if (ctas == 2) return pick_staged_ct<D, kBF16, 2>(steps, stages);
+  if (ctas == 4) return pick_staged_ct<D, kBF16, 4>(steps, stages);
   return nullptr;
 }
 

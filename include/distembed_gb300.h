@@ -62,7 +62,8 @@ typedef struct de_options {
 } de_options;
 
 /* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5,
- * automatic edge cap, programmatic dependent launch on. */
+ * automatic edge cap, programmatic dependent launch on, negatives staged in shared
+ * memory. */
 void de_default_options(de_options *o);
 
 /* Uploads the CSR (n vertices, nnz entries) and prepares a handle for embeddings of
@@ -173,7 +174,7 @@ int de_batch_get_embeddings_f32(de_batch *b, int32_t graph, float *x);
  *                      vertices_per_warp (1, 2 or 4) items at once on 32, 16 or 8
  *                      lanes; team_warps 4, 8, 16 or 32; edge_cap 1..4096
  *   DE_BATCH_STAGED    every warp stages the rows of its next stages-1 chunks in
- *                      shared memory with bulk asynchronous copies; a pair is
+ *                      shared memory with 16-byte asynchronous copies; a pair is
  *                      computed by dim/8 lanes; team_warps 2..16; edge_cap 1..32
  *                      (one chunk); pairs = warp steps in flight (1 or 2);
  *                      stages 3 or 4 ring slots per warp; at most 32 negatives
@@ -192,9 +193,10 @@ typedef struct de_batch_shape {
   int32_t edge_cap;          /* CSR entries per work item                    */
   int32_t pairs;             /* staged kernel: warp steps in flight          */
   int32_t stages;            /* staged kernel                                */
-  int32_t team_ctas;         /* staged kernel: 2 = the largest graphs are     */
-                             /* trained by the two CTAs of a cluster together */
-                             /* (the rest one per CTA); 0 or 1 = one CTA each */
+  int32_t team_ctas;         /* staged kernel: 2 or 4 = the largest graphs    */
+                             /* are trained by the CTAs of a cluster of that  */
+                             /* size together (the rest one per CTA); 0 or 1  */
+                             /* = one CTA each                                */
 } de_batch_shape;
 int de_batch_set_shape(de_batch *b, const de_batch_shape *shape);
 int de_batch_get_shape(const de_batch *b, de_batch_shape *shape);

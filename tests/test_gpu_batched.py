@@ -107,7 +107,7 @@ SHAPES = [dict(kernel="register", vertices_per_warp=1, team_warps=4, edge_cap=32
           dict(kernel="rows", team_warps=4, edge_cap=8, pairs=2, stages=4),
           dict(kernel="rows", team_warps=2, edge_cap=32, pairs=2, stages=3),
           dict(kernel="rows", team_warps=3, edge_cap=1, pairs=1, stages=4),
-          CLUSTER, dict(CLUSTER, team_warps=4, edge_cap=8, pairs=1, stages=4)]
+          CLUSTER, dict(CLUSTER, team_warps=4, edge_cap=8, pairs=1, stages=4), dict(CLUSTER, team_ctas=4)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "-".join(str(v) for v in s.values()))
@@ -253,12 +253,14 @@ def test_hub_rows_and_many_chunks_per_warp(shape):
     assert np.all(np.abs(loss[0] - lo) <= LOSS_RTOL * lo)
 
 
-def test_cluster_teams_match_single_cta_teams_bitwise():
-    # the largest graphs of a mix go to two-CTA teams; every graph's result is the
-    # same as with one CTA per graph (same items, same order of every sum)
+@pytest.mark.parametrize("ctas", [2, 4])
+def test_cluster_teams_match_single_cta_teams_bitwise(ctas):
+    # the largest graphs of a mix go to teams of two or four CTAs of a cluster;
+    # every graph's result is the same as with one CTA per graph (same items, same
+    # order of every sum)
     dim, E, B, ns = 64, 3, 256, 5
     one = dict(CLUSTER, team_ctas=1)
     xs1, l1 = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=one)
-    xs2, l2 = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=CLUSTER)
+    xs2, l2 = run_batch(GRAPHS, dim, E, B, ns, 0.02, precision="bf16", shape=dict(CLUSTER, team_ctas=ctas))
     for i in range(len(GRAPHS)):
         assert np.array_equal(xs1[i], xs2[i]) and np.array_equal(l1[i], l2[i]), i
