@@ -95,7 +95,8 @@ __device__ __forceinline__ void pair_steps(const BatchedArgs &a, float (&acc)[8]
       loss += kAttract ? __logf(1.0f + r[st]) : __logf(1.0f + r[st]) - __logf(r[st] + 1e-6f);
     may_clip |= c[st] * c[st] * r[st] > 0.98f * a.bound * a.bound;
   }
-  if (!__any_sync(kAll, may_clip)) {
+  // attractive pairs never clip at bound >= 1 (2 sqrt(r) / (1 + r) <= 1): no vote
+  if ((kAttract && a.bound >= 1.0f) || !__any_sync(kAll, may_clip)) {
 #pragma unroll
     for (int st = 0; st < NS; ++st) {
       axpy8(acc, lr * c[st], d[st]);
@@ -295,14 +296,18 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
               reinterpret_cast<float4 *>(dst + gl * 8)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
             }
 #pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kAll, loss, m);
-            if (lane == 0) item_loss[tw + (r0 + k) * TW] = loss;
+            if (want) {
+#pragma unroll
+              for (int m = 16; m >= 1; m >>= 1) loss += __shfl_xor_sync(kAll, loss, m);
+              if (lane == 0) item_loss[tw + (r0 + k) * TW] = loss;
+            }
             __syncwarp();
           }
         }
         dev::cp_async_wait<0>();
         team_sync();
-        combine_split_rows<D>(a, slots, stage, a.batch_split_off[bi], a.batch_split_off[bi + 1], tw, TW, lane);
+        const int s0 = a.batch_split_off[bi], s1 = a.batch_split_off[bi + 1];
+        combine_split_rows<D>(a, slots, stage, s0, s1, tw, TW, lane);
         // the minibatch's loss in item order (rank 0, warp 0), whatever team made it
         if (want && trank == 0 && warp == 0) {
           double l = 0.0;
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
           for (int m = 16; m >= 1; m >>= 1) l += __shfl_xor_sync(kAll, l, m);
           eloss += l;
         }
-        team_sync();
+        if (s1 > s0) team_sync();  // combined split rows are staged before the update reads them
         update_rows<kBF16>(a.xm, a.xb, stage, (G.voff + base) * D, rows * D, trank * blockDim.x + threadIdx.x,
                            nct * blockDim.x);  // algo.hpp:651-666
         team_sync();
