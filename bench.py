@@ -73,7 +73,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pdl", type=int, default=1, help="plain form: overlap consecutive minibatch launches")
     p.add_argument("--edge-cap", type=int, default=0, help="plain form: max CSR entries per work item (0: automatic)")
-    p.add_argument("--stage-negs", type=int, default=1,
+    p.add_argument("--stage-negs", type=int, default=0,
                    help="plain form: 1 copies the negative rows into shared memory (bulk copies) per CTA")
     p.add_argument("--form", default="headline",
                    choices=["headline", "plain", "knn20k", "bf16", "batched", "served", "spmm", "sparse"],
@@ -83,8 +83,9 @@ def parse():
     p.add_argument("--jobs", type=int, default=256, help="served form: jobs in the arrival stream")
     p.add_argument("--scale", type=int, default=0, help="bf16 form: R-MAT scale instead of 22 (small profiling cases)")
     p.add_argument("--slots", type=int, default=16, help="served form: jobs in flight at most")
-    p.add_argument("--served-precision", default="bf16", choices=["bf16", "fp32"],
-                   help="served form: storage of the jobs (dim 32 jobs run FP32: the BF16 form takes 64-256)")
+    p.add_argument("--served-precision", default="fp32", choices=["bf16", "fp32"],
+                   help="served form: storage of the jobs (dim 32 jobs run FP32: the BF16 form takes 64-256); "
+                        "FP32 serves this stream faster (5 negatives: the BF16 form's GEMMs do not pay)")
     p.add_argument("--no-plain-compare", action="store_true", help="batched form: skip the FP32 plain comparison")
     p.add_argument("--no-served", action="store_true", help="headline: skip the served legs")
     p.add_argument("--no-gap", action="store_true", help="skip the FP64 oracle runs (loss gaps)")
@@ -825,7 +826,7 @@ def roofline_batched(graphs, step_ms, precision="bf16"):
         * W4["epochs"]
     mean_s = statistics.mean(step_ms) / 1e3
     peak, peak_kind = measured_peak()
-    traffic = profile_traffic("batched_kernel_batched512.txt")
+    traffic = profile_traffic("staged_kernel_batched512.txt")
     achieved = alg / mean_s / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "traffic": traffic, "kernel": "staged_kernel (batched, persistent)",
@@ -1389,15 +1390,18 @@ def run_headline(args):
             jobs = served_workload(args.jobs, f"cuda:{local}")
             x0_of = ServedStart(jobs)
             full, half = served_pair(jobs, x0_of, args.slots, args.served_precision, local)
+            other = "fp32" if args.served_precision == "bf16" else "bf16"
+            full_other = served_leg(jobs, x0_of, args.slots, other, 1.0, local)
             gaps = [] if args.no_gap else served_oracle_gaps(jobs, x0_of, full["final_loss"])
-            for leg in (full, half):
+            for leg in (full, half, full_other):
                 leg.pop("final_loss")
                 leg.pop("clocks", None)
             served = {"workload": f"served{len(jobs)}_poisson200: Poisson arrivals 200 jobs/s (seed 4), n "
                                   "log-uniform [1000, 2e6], R-MAT ef 8 or kNN k=10 (kNN up to 1e5 vertices), dim in "
                                   "{32, 64, 128}, 10-50 epochs, minibatch 16384, 5 negatives, lr 0.02",
-                      "storage": f"{args.served_precision} (dim 32 jobs FP32)",
+                      "storage": f"{args.served_precision} (BF16 only for jobs of dim 64-256; dim 32 jobs FP32)",
                       "at_config_rate": full, "at_half_capacity": half,
+                      f"at_config_rate_{other}": full_other,
                       "final_gap_vs_fp64_oracle_smallest_knn_jobs": gaps,
                       "served_vs_alone": "bitwise equal (tests/test_gpu_served.py)"}
     if rank == 0:

@@ -257,7 +257,7 @@ class Handle:
 
     def __init__(self, rowptr, col, dim: int, precision: str = "fp32", quirks: bool = True,
                  compute_loss: bool = True, device: int = 0, stream: int | None = None,
-                 max_bound: float = 5.0, edge_cap: int = 0, pdl: bool = True, stage_negatives: bool = True):
+                 max_bound: float = 5.0, edge_cap: int = 0, pdl: bool = True, stage_negatives: bool = False):
         L = lib()
         self._rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
         self._col = np.ascontiguousarray(col, dtype=np.int64)

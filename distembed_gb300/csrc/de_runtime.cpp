@@ -553,7 +553,6 @@ void de_default_options(de_options *o) {
   o->max_bound = 5.0;
   o->edge_cap = 0;
   o->pdl = 1;
-  o->stage_negatives = 1;
 }
 
 int de_create(int64_t n, const int64_t *rowptr, const int64_t *col, int64_t nnz, int32_t dim,

@@ -62,8 +62,8 @@ typedef struct de_options {
 } de_options;
 
 /* Fills *o with the defaults: FP32, quirks on, loss on, device 0, own stream, bound 5,
- * automatic edge cap, programmatic dependent launch on, negatives staged in shared
- * memory. */
+ * automatic edge cap, programmatic dependent launch on, negatives read from L1/L2
+ * (the shared-memory staging measured 8.5% slower at R-MAT scale 20). */
 void de_default_options(de_options *o);
 
 /* Uploads the CSR (n vertices, nnz entries) and prepares a handle for embeddings of
