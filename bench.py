@@ -742,10 +742,17 @@ def batched_leg(graphs, x0_all, precision, local, steps, warmup, e2e_steps=0, sh
         b.prepare(E, B, ns, lr)
     b.close()
     span = trace[:, 1] - trace[:, 0]
+    ends = {}
+    for t, e in zip(trace[:, 2].tolist(), trace[:, 1].tolist()):
+        ends[t] = max(ends.get(t, 0), e)
+    ends = np.array(sorted(ends.values()), dtype=np.float64) / 1e6
     return {"edge_updates": upd, "step_ms": step_ms, "value": upd * len(step_ms) / (sum(step_ms) / 1e3), "loss": loss,
             "shape": shape, "tuned": tuned, "tune_s": tune_s, "e2e": e2e, "clocks": clk,
             "trace": {"makespan_ms": float(trace[:, 1].max()) / 1e6, "longest_graph_ms": float(span.max()) / 1e6,
-                      "graph_ms_sum": float(span.sum()) / 1e6, "teams": int(len(np.unique(trace[:, 2])))}}
+                      "graph_ms_sum": float(span.sum()) / 1e6, "teams": int(len(np.unique(trace[:, 2]))),
+                      "team_end_ms_p10_p50_p90": [float(np.percentile(ends, q)) for q in (10, 50, 90)],
+                      "note": "the launch that computes every epoch's loss (the timed ones compute the last "
+                              "epoch's only)"}}
 
 
 def plain_same_graphs(graphs, x0, local):

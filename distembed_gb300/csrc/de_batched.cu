@@ -35,9 +35,11 @@ namespace {
 // Largest dynamic shared memory a staged team may use (the static part is small).
 constexpr size_t kStagedSmemMax = 227 * 1024 - 1024;
 
+// Dynamic shared memory of a staged team with (ids = 1) or without its column-id
+// buffers.
 template <int D, bool kBF16>
-size_t staged_smem(const de_batch_shape &s, int ns) {
-  return StagedLayout<D, kBF16>::bytes(s.team_warps, s.stages, s.edge_cap, ns);
+size_t staged_smem(const de_batch_shape &s, int ns, int ids) {
+  return StagedLayout<D, kBF16>::bytes(s.team_warps, s.stages, s.edge_cap, ns, ids);
 }
 
 template <int D, bool kBF16>
@@ -52,6 +54,7 @@ struct KernelPick {
   int block = 0;
   size_t smem = 0;
   int ctas = 1;  // CTAs per cluster the kernel is launched with
+  int stage_ids = 0;  // staged kernel: the column-id buffers fit in shared memory
 };
 
 KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) {
@@ -88,20 +91,19 @@ KernelPick pick_kernel(int dim, bool bf16, const de_batch_shape &s, int ns = 0) 
     k.block = 32 * s.team_warps;
     return k;
   }
-  switch (dim) {
-    case 32:
-      k.fn = pick_staged(32, bf16, s.pairs, s.stages, k.ctas);
-      k.smem = bf16 ? staged_smem<32, true>(s, ns) : staged_smem<32, false>(s, ns);
-      break;
-    case 64:
-      k.fn = pick_staged(64, bf16, s.pairs, s.stages, k.ctas);
-      k.smem = bf16 ? staged_smem<64, true>(s, ns) : staged_smem<64, false>(s, ns);
-      break;
-    case 128:
-      k.fn = pick_staged(128, bf16, s.pairs, s.stages, k.ctas);
-      k.smem = bf16 ? staged_smem<128, true>(s, ns) : staged_smem<128, false>(s, ns);
-      break;
-  }
+  auto smem_of = [&](int ids) -> size_t {
+    switch (dim) {
+      case 32: return bf16 ? staged_smem<32, true>(s, ns, ids) : staged_smem<32, false>(s, ns, ids);
+      case 64: return bf16 ? staged_smem<64, true>(s, ns, ids) : staged_smem<64, false>(s, ns, ids);
+      case 128: return bf16 ? staged_smem<128, true>(s, ns, ids) : staged_smem<128, false>(s, ns, ids);
+    }
+    return 0;
+  };
+  k.fn = pick_staged(dim, bf16, s.pairs, s.stages, k.ctas);
+  // the column-id buffers where they fit; without them the kernel reads the ids
+  // from global memory one chunk ahead
+  k.stage_ids = smem_of(1) <= kStagedSmemMax ? 1 : 0;
+  k.smem = smem_of(k.stage_ids);
   if (k.smem > kStagedSmemMax) k.fn = nullptr;
   k.block = 32 * s.team_warps;
   return k;
@@ -396,6 +398,7 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
   a.cluster_slot = b->d_cluster_slot;
   a.item_loss = b->d_item_loss;
   a.item_stride = b->max_batch_items;
+  a.stage_ids = k.stage_ids;
   b->ctas = k.ctas;
   b->kernel = k.fn;
   b->teams = teams;

@@ -64,6 +64,7 @@ struct BatchedArgs {
   float *item_loss;          // [teams, max items of a minibatch] loss of every work item
   int32_t item_stride;
   int32_t loss_from;         // epochs e >= loss_from (of this run) compute their loss; the others write 0
+  int32_t stage_ids;         // staged kernel: 1 = a round's column ids are prefetched into shared memory
 };
 
 static __device__ __forceinline__ long long globaltimer() {
@@ -152,11 +153,15 @@ struct StagedLayout {
   static constexpr int kRowB = kBF16 ? 2 * D : 4 * D;  // a neighbour row in shared memory
   static constexpr int kXiB = 4 * D;                   // the chunk's own row (FP32 master)
   __host__ __device__ static constexpr int slot_bytes(int cap) { return kXiB + cap * kRowB; }
-  // per warp: S slots, the negatives (ns rows), 32 work items
-  __host__ __device__ static size_t warp_bytes(int S, int cap, int ns) {
-    return size_t(S) * slot_bytes(cap) + size_t(ns) * kRowB + 32 * sizeof(WorkItem);
+  // per warp: S slots, the negatives (ns rows), 32 work items and, with ids = 1,
+  // their column ids (cap per item, 16-byte aligned)
+  __host__ __device__ static size_t warp_bytes(int S, int cap, int ns, int ids = 1) {
+    return size_t(S) * slot_bytes(cap) + size_t(ns) * kRowB + 32 * sizeof(WorkItem) +
+           (ids ? ((size_t(32) * cap * 4 + 15) & ~size_t(15)) : 0);
   }
-  __host__ __device__ static size_t bytes(int W, int S, int cap, int ns) { return size_t(W) * warp_bytes(S, cap, ns); }
+  __host__ __device__ static size_t bytes(int W, int S, int cap, int ns, int ids = 1) {
+    return size_t(W) * warp_bytes(S, cap, ns, ids);
+  }
 };
 
 // Copies `rows` rows (ids: lane j holds row j's vertex, local to voff) of

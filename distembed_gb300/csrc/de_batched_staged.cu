@@ -158,9 +158,11 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
   const int W = blockDim.x >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gl = lane % LP;
   const int cap = a.cap, slotB = Lay::slot_bytes(cap);
-  unsigned char *ring = smem + size_t(warp) * Lay::warp_bytes(S, cap, a.ns);
+  unsigned char *ring = smem + size_t(warp) * Lay::warp_bytes(S, cap, a.ns, a.stage_ids);
   unsigned char *negrows = ring + size_t(S) * slotB;
   WorkItem *my_items = reinterpret_cast<WorkItem *>(negrows + size_t(a.ns) * kRowB);
+  const int *colbuf = reinterpret_cast<const int *>(my_items + 32);  // [32][cap] column ids of the round
+  const uint32_t colbuf_s = dev::smem_u32(colbuf);
   const uint32_t ring_s = dev::smem_u32(ring), neg_s = dev::smem_u32(negrows);
   __shared__ int sh_graph;
   const unsigned char *src = kBF16 ? reinterpret_cast<const unsigned char *>(a.xb)
@@ -230,12 +232,28 @@ __global__ void __launch_bounds__(512, 1) staged_kernel(const BatchedArgs a) {
         const int nmine = n_items > tw ? (n_items - tw + TW - 1) / TW : 0;
         for (int r0 = 0; r0 < nmine; r0 += 32) {
           const int nr = min(32, nmine - r0);
-          if (lane < nr) my_items[lane] = a.items[it0 + tw + int64_t(r0 + lane) * TW];
+          // the round's work items, and every column id they read, fetched at once
+          // (row l of colbuf: item l's CSR entries, 4-byte asynchronous copies), so
+          // that no chunk waits on its column ids
+          if (lane < nr) {
+            const WorkItem mine = a.items[it0 + tw + int64_t(r0 + lane) * TW];
+            my_items[lane] = mine;
+            if (a.stage_ids) {
+              const int32_t *cs = a.col + G.eoff + mine.e_begin;
+              const uint32_t dst = colbuf_s + uint32_t(lane * cap * 4);
+              for (int i = 0; i < mine.e_end - mine.e_begin; ++i) dev::cp_async4(dst + 4u * i, cs + i);
+            }
+          }
+          if (a.stage_ids) {
+            dev::cp_async_commit();
+            dev::cp_async_wait<0>();
+          }
           __syncwarp();
           // lane l: column id of CSR entry l of chunk k (-1 past its end)
           auto load_cols = [&](int k) -> int {
             const WorkItem &it = my_items[k];
-            return lane < it.e_end - it.e_begin ? __ldg(a.col + G.eoff + it.e_begin + lane) : -1;
+            if (lane >= it.e_end - it.e_begin) return -1;
+            return a.stage_ids ? colbuf[k * cap + lane] : __ldg(a.col + G.eoff + it.e_begin + lane);
           };
           auto issue = [&](int k, int id) {
             const uint32_t slot = ring_s + uint32_t((k % S) * slotB);
