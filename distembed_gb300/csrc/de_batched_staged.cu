@@ -12,10 +12,12 @@ namespace {
 // registers, and the copies of later chunks overlap the arithmetic of the current
 // one.  Every warp runs its own pipeline over its chunks (work items i = warp,
 // warp + W, ... of the minibatch; a chunk is at most cap <= 32 CSR entries):
-//   column ids of chunk k+S are loaded while the rows of chunk k+S-1 are copied
-//   (own row from the FP32 master, neighbours from the BF16 copy or the FP32
-//   master) into ring slot (k+S-1) mod S, and chunk k is computed from slot k mod S
-//   once its copy group has landed (cp.async.wait_group S-1).
+//   a round of up to 32 items starts by fetching all their column ids into shared
+//   memory (4-byte cp.async; where that buffer does not fit, chunk k+S's ids are
+//   loaded from global memory one chunk ahead instead), then the rows of chunk
+//   k+S-1 are copied (own row from the FP32 master, neighbours from the BF16 copy
+//   or the FP32 master) into ring slot (k+S-1) mod S while chunk k is computed from
+//   slot k mod S once its copy group has landed (cp.async.wait_group S-1).
 // Each warp also copies the minibatch's ns negatives into its own area (with its
 // first chunk).  A pair is computed by dim/8 lanes (8 components each),
 // 32/(dim/8) pairs per warp step and NS steps in flight.  Results go to the
