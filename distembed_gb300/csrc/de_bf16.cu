@@ -18,7 +18,7 @@
 // per-row bitmask; the update kernel adds those pairs one by one in FP32 with
 // the clip.
 //
-// Per minibatch: bf16_gather_kernel (the negatives into N, N^T, |n|^2), then
+// Per minibatch: bf16_gather_kernel (the negatives into N, |n|^2), then
 // bf16_attract_kernel (attractive pass, warp per work item) and
 // bf16_repulse_kernel (the GEMMs), which are independent and run on two
 // streams, then bf16_apply_kernel (exact close pairs and the update of every
@@ -118,15 +118,14 @@ __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D>
   if (mask) pair_forces<D, U, true>(acc, xi, xn, mask, lr, bound, want_loss, loss, lane);
 }
 
-// The minibatch's negatives gathered once: N (k x dim), N^T (dim x k), |n|^2 and
-// ids.  A CTA takes 32 consecutive negatives, one warp each: the warp copies its
-// row into N and a shared tile (D/32 components per lane), then thread d writes
-// dim d's 32 values of N^T as 64 contiguous bytes.
+// The minibatch's negatives gathered once: N (k x dim, zero rows for padding),
+// |n|^2 and ids.  A CTA takes 32 consecutive negatives, one warp each: the warp
+// copies its row into N (D/32 components per lane) and reduces |n|^2.
 constexpr int kGatherTile = 32;
 template <int D>
 __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF16BatchArgs a) {
   constexpr int N = D / 32;  // components per lane
-  __shared__ __align__(16) __nv_bfloat16 tile[kGatherTile][D];
+  pdl_trigger();  // the repulsion GEMMs may start their prologue (they wait before reading N)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int epoch = a.epoch[0];
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
@@ -139,7 +138,6 @@ __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF1
     if constexpr (N == 8) {
       uint4 u = n >= 0 ? __ldg(reinterpret_cast<const uint4 *>(a.xb + size_t(n) * D) + lane) : make_uint4(0, 0, 0, 0);
       reinterpret_cast<uint4 *>(a.nb + size_t(k) * D)[lane] = u;
-      reinterpret_cast<uint4 *>(&tile[kk][0])[lane] = u;
       const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -149,7 +147,6 @@ __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF1
     } else if constexpr (N == 4) {
       uint2 u = n >= 0 ? __ldg(reinterpret_cast<const uint2 *>(a.xb + size_t(n) * D) + lane) : make_uint2(0, 0);
       reinterpret_cast<uint2 *>(a.nb + size_t(k) * D)[lane] = u;
-      reinterpret_cast<uint2 *>(&tile[kk][0])[lane] = u;
       const uint32_t w[2] = {u.x, u.y};
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
@@ -160,7 +157,6 @@ __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF1
       static_assert(N == 2, "dim 64, 128 or 256");
       uint32_t u = n >= 0 ? __ldg(reinterpret_cast<const uint32_t *>(a.xb + size_t(n) * D) + lane) : 0u;
       reinterpret_cast<uint32_t *>(a.nb + size_t(k) * D)[lane] = u;
-      reinterpret_cast<uint32_t *>(&tile[kk][0])[lane] = u;
       const float lo = __uint_as_float(u << 16), hi = __uint_as_float(u & 0xffff0000u);
       sq = fmaf(lo, lo, hi * hi);
     }
@@ -170,18 +166,6 @@ __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF1
       a.nn[k] = n >= 0 ? sq : __int_as_float(0x7f800000);  // no draw: |n|^2 = +inf, so c = 0
       a.nid[k] = n;
     }
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < D; d += blockDim.x) {
-    uint32_t w[kGatherTile / 2];
-#pragma unroll
-    for (int i = 0; i < kGatherTile / 2; ++i) {
-      const uint32_t lo = __bfloat16_as_ushort(tile[2 * i][d]), hi = __bfloat16_as_ushort(tile[2 * i + 1][d]);
-      w[i] = lo | (hi << 16);
-    }
-    uint4 *dst = reinterpret_cast<uint4 *>(a.nbt + size_t(d) * a.kpad + k0);
-#pragma unroll
-    for (int i = 0; i < kGatherTile / 8; ++i) dst[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
   }
 }
 
@@ -249,9 +233,19 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
          (uint64_t(2) << 61);
 }
 
-// Instruction descriptor: BF16 x BF16 -> FP32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+// The same swizzled atoms read as an MN-major operand (B of the second GEMM: the
+// rows of a chunk of N are its K index, their 64-dim atoms its N index): lbo =
+// bytes between 64-element atoms along N, sbo = bytes between 8-row groups along K.
+__device__ __forceinline__ uint64_t umma_desc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((addr & 0x3FFFF) >> 4) | (uint64_t(lbo >> 4) << 16) | (uint64_t(sbo >> 4) << 32) |
+         (uint64_t(1) << 46) | (uint64_t(2) << 61);
+}
+
+// Instruction descriptor: BF16 x BF16 -> FP32, M x N, A K-major, B K-major or
+// (b_mn) MN-major.
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n, bool b_mn = false) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (b_mn ? (1u << 16) : 0u) | (uint32_t(n >> 3) << 17) |
+         (uint32_t(m >> 4) << 24);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
@@ -294,14 +288,13 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 template <int D>
 struct RepulseSmem {
   static constexpr int kAtoms = D / 64;                  // 128-B column atoms of a dim-wide row
+  static constexpr int kStages = 4;                      // chunks of N in flight
   static constexpr int kX = kAtoms * kTileRows * 128;    // X tile
-  static constexpr int kN = kAtoms * kChunk * 128;       // one chunk of N
-  static constexpr int kT = D * 128;                     // one chunk of N^T (D rows x 64 negatives)
+  static constexpr int kN = kAtoms * kChunk * 128;       // one chunk of N (operand of both GEMMs)
   static constexpr int kC = kTileRows * 128;             // one chunk of C (128 rows x 64 coefficients)
   static constexpr int offX = 0;
   static constexpr int offN = offX + kX;
-  static constexpr int offT = offN + 2 * kN;
-  static constexpr int offC = offT + 2 * kT;
+  static constexpr int offC = offN + kStages * kN;
   static constexpr int bytes = offC + 2 * kC;
   static constexpr int dynamic = bytes + 1024;           // + alignment slack
 };
@@ -310,16 +303,19 @@ struct RepulseSmem {
 // Epilogue warp w serves TMEM lane quadrant w % 4 (tile rows 32(w%4) .. +31) and
 // column half w / 4: 32 of the 64 coefficients of each chunk, and half of the
 // dims in the final update.  TMEM: S chunks in columns [0, 128) (double
-// buffered), F in columns [256, 256 + dim).
+// buffered), F in columns [256, 256 + dim).  Chunks of N stream through a ring
+// of four shared-memory stages; each stage is the B operand of both GEMMs (K-
+// major for S = X N^T, MN-major for F += C N), so no transposed copy exists.
 //
 // KS = 2: the negatives of a tile are split between the two CTAs of a cluster
 // (rank 0: the first ceil(chunks / 2) chunks, rank 1 the rest), so twice as
-// many SMs work on a minibatch.  Each CTA stages its partial force
-// (its row sums) x - (its F); after a cluster barrier rank r adds the peer's
-// staged rows (read through distributed shared memory) for tile rows
-// [64 r, 64 r + 64) and stores them, and a second cluster barrier keeps both
-// CTAs' shared memory alive until the peer has read it.  Partial sums are
-// combined as own + peer, which is the same value on either rank.
+// many SMs work on a minibatch.  Rank r owns tile rows [64 r, 64 r + 64).  After
+// a cluster barrier (both CTAs done with their operand buffers) each CTA stages
+// its partial force (its row sums) x - (its F) of the rows it owns locally and
+// pushes those of the peer's rows into the peer's shared memory (posted stores
+// through distributed shared memory); after a second cluster barrier each CTA
+// adds the two partials of its rows from its own shared memory and stores them.
+// Partial sums are combined as own + peer, the same value on either rank.
 constexpr int kEpiThreads = 256;
 constexpr int kRepulseThreads = kEpiThreads + 64;
 
@@ -328,41 +324,54 @@ __device__ __forceinline__ int cta_rank_in_cluster() {
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
   return r;
 }
-// Every thread of both CTAs arrives (release) and waits (acquire).
-__device__ __forceinline__ void cluster_barrier() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+// Release arrive on a barrier of the peer CTA (address from peer_addr).
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// mbar_wait with cluster-scope acquire (the phase was completed by the peer CTA).
+__device__ __forceinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity, int *err_shared) {
+  for (long it = 0; it < kSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*reinterpret_cast<volatile int *>(err_shared)) return false;
+  }
+  *reinterpret_cast<volatile int *>(err_shared) = 1;
+  return false;
 }
 __device__ __forceinline__ uint32_t peer_addr(uint32_t local, int peer) {
   uint32_t r;
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(peer));
   return r;
 }
-__device__ __forceinline__ float2 ld_peer_f2(uint32_t addr) {
-  float2 v;
-  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
-  return v;
-}
-__device__ __forceinline__ double ld_peer_f64(uint32_t addr) {
-  double v;
-  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
-  return v;
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// this CTA's shared memory into the peer CTA's (dst, bar: peer_addr addresses),
+// completing on the peer's barrier.
+__device__ __forceinline__ void bulk_s2peer(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "r"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
 template <int D, int KS>
 __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const __grid_constant__ CUtensorMap map_x,
                                                                const __grid_constant__ CUtensorMap map_n,
-                                                               const __grid_constant__ CUtensorMap map_t,
                                                                const BF16BatchArgs a) {
   using L = RepulseSmem<D>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ __align__(8) uint64_t bar[18];
+  __shared__ __align__(8) uint64_t bar[21];
   __shared__ uint32_t tmem_holder;
   __shared__ int err;
   __shared__ float2 negmeta[2][kChunk];  // (|n|^2, vertex id) of a chunk's negatives
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = a.kpad / kChunk;
   const int ks = KS == 2 ? cta_rank_in_cluster() : 0;
+  const int peer = ks ^ 1;  // KS = 2: the other CTA of the cluster
   const int tile_base = (blockIdx.x / KS) * kTileRows;  // row offset within the minibatch
   // this CTA's chunks [c_begin, c_end) (KS = 2 needs at least two chunks)
   const int c_begin = ks == 0 ? 0 : (nchunks + 1) / 2;
@@ -370,26 +379,32 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   const int nloc = c_end - c_begin;
 
   // barrier ids
+  constexpr int NST = L::kStages;
   const uint32_t b0 = smem_u32(&bar[0]);
   auto B = [&](int i) { return b0 + 8u * uint32_t(i); };
-  const int FULL_X = 0, FULL_N = 1, FULL_T = 3, FREE_N = 5, FREE_T = 7, S_FULL = 9, S_FREE = 11, C_FULL = 13,
-            C_FREE = 15, F_DONE = 17;
+  const int FULL_X = 0, FULL_N = 1, FREE_N = FULL_N + NST, S_FULL = FREE_N + NST, S_FREE = S_FULL + 2,
+            C_FULL = S_FREE + 2, C_FREE = C_FULL + 2, F_DONE = C_FREE + 2, INCOMING = F_DONE + 1,
+            PEER_FREE = INCOMING + 1, PEER_GOT = PEER_FREE + 1;
+  static_assert(1 + 2 * NST + 8 + 4 <= 21, "barrier slots");
   auto failed = [&]() { return *reinterpret_cast<volatile int *>(&err) != 0; };
 
   if (tid == 0) {
     err = 0;
     mbar_init(B(FULL_X), 1);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NST; ++i) {
       mbar_init(B(FULL_N + i), 1);
-      mbar_init(B(FULL_T + i), 1);
       mbar_init(B(FREE_N + i), 1);
-      mbar_init(B(FREE_T + i), 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(B(S_FULL + i), 1);
       mbar_init(B(S_FREE + i), kEpiThreads);
       mbar_init(B(C_FULL + i), kEpiThreads);
       mbar_init(B(C_FREE + i), 1);
     }
     mbar_init(B(F_DONE), 1);
+    mbar_init(B(INCOMING), 1);
+    mbar_init(B(PEER_FREE), 1);
+    mbar_init(B(PEER_GOT), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 9) {
@@ -401,46 +416,53 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  // KS = 2: every thread arrives once here, after the barrier initialisation,
+  // and waits once before this CTA first touches the peer's shared memory
+  if constexpr (KS == 2) asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
   const uint32_t tmem = tmem_holder;
   const uint32_t sX = smem_u32(sm + L::offX);
-  auto sN = [&](int b) { return smem_u32(sm + L::offN + b * L::kN); };
-  auto sT = [&](int b) { return smem_u32(sm + L::offT + b * L::kT); };
+  auto sN = [&](int st) { return smem_u32(sm + L::offN + st * L::kN); };
   unsigned char *sC_ptr[2] = {sm + L::offC, sm + L::offC + L::kC};
   // after the GEMMs: the staged force rows (pitch D + 4 floats) over the operand
   // buffers (at dim 256 reaching into C[0]); per tile row a flag (nonzero: the
   // row's force is final) and, with KS = 2, its loss, both in C[1]
   constexpr int kPitch = D + 4;
-  constexpr int kPer = D / 32;  // dims per lane in the row stores
   float *const stage = reinterpret_cast<float *>(sm + L::offN);
-  static_assert(kTileRows * kPitch * 4 <= 2 * (L::kN + L::kT) + L::kC, "staging fits before C[1]");
+  // KS = 2: the peer's partials of this CTA's 64 rows arrive in the X tile
+  // (pitch D floats), their 64 flags and 64 losses in C[1] after the own ones
+  static_assert(64 * D * 4 == L::kX, "the incoming rows fill the X tile");
+  int *const in_flags = reinterpret_cast<int *>(sC_ptr[1] + 4096);
+  double *const in_loss = reinterpret_cast<double *>(sC_ptr[1] + 8192);
+  constexpr uint32_t kInBytes = 64 * D * 4 + 64 * 4 + 64 * 8;
+  static_assert(kTileRows * kPitch * 4 <= NST * L::kN + L::kC, "staging fits before C[1]");
   int *const row_flags = reinterpret_cast<int *>(sC_ptr[1]);
   double *const row_loss = reinterpret_cast<double *>(sC_ptr[1] + 1024);
 
   if (warp == 8) {
     // ---------------- TMA producer
     if (lane == 0) {
-      int issued_n[2] = {0, 0}, issued_t[2] = {0, 0};
+      int issued_n[NST] = {};
       mbar_expect_tx(B(FULL_X), L::kX);
       for (int ka = 0; ka < L::kAtoms; ++ka)
         tma_load_2d(sX + ka * kTileRows * 128, &map_x, ka * 64, a.base + tile_base, B(FULL_X));
+      // N comes from bf16_gather_kernel (launched just before, possibly still
+      // running under a programmatic dependency): wait for it
+      pdl_wait();
+      // chunk lc into stage lc % NST once the second GEMM of chunk lc - NST has
+      // read that stage
       for (int lc = 0; lc < nloc && !failed(); ++lc) {
-        const int c = c_begin + lc, b = lc & 1;
-        if (lc >= 2 && !mbar_wait(B(FREE_N + b), ((lc >> 1) + 1) & 1, &err)) break;
-        mbar_expect_tx(B(FULL_N + b), L::kN);
-        for (int ka = 0; ka < L::kAtoms; ++ka) tma_load_2d(sN(b) + ka * kChunk * 128, &map_n, ka * 64, c * kChunk, B(FULL_N + b));
-        ++issued_n[b];
-        if (lc >= 2 && !mbar_wait(B(FREE_T + b), ((lc >> 1) + 1) & 1, &err)) break;
-        mbar_expect_tx(B(FULL_T + b), L::kT);
-        tma_load_2d(sT(b), &map_t, c * kChunk, 0, B(FULL_T + b));
-        ++issued_t[b];
+        const int c = c_begin + lc, st = lc % NST, use = lc / NST;
+        if (use > 0 && !mbar_wait(B(FREE_N + st), (use - 1) & 1, &err)) break;
+        mbar_expect_tx(B(FULL_N + st), L::kN);
+        for (int ka = 0; ka < L::kAtoms; ++ka)
+          tma_load_2d(sN(st) + ka * kChunk * 128, &map_n, ka * 64, c * kChunk, B(FULL_N + st));
+        ++issued_n[st];
       }
       if (failed()) {
         // bounded wait for every copy this thread started before the CTA leaves
         int dummy = 0;
-        for (int b = 0; b < 2; ++b) {
-          if (issued_n[b]) mbar_wait(B(FULL_N + b), (issued_n[b] - 1) & 1, &dummy);
-          if (issued_t[b]) mbar_wait(B(FULL_T + b), (issued_t[b] - 1) & 1, &dummy);
-        }
+        for (int st = 0; st < NST; ++st)
+          if (issued_n[st]) mbar_wait(B(FULL_N + st), (issued_n[st] - 1) & 1, &dummy);
         mbar_wait(B(FULL_X), 0, &dummy);
       }
     }
@@ -448,33 +470,34 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     // ---------------- MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc1 = umma_idesc(kTileRows, kChunk);
-      constexpr uint32_t idesc2 = umma_idesc(kTileRows, D);
+      constexpr uint32_t idesc2 = umma_idesc(kTileRows, D, true);
       const uint32_t tmem_f = tmem + 256;
       bool ok = mbar_wait(B(FULL_X), 0, &err);
+      // F += C N: B is the chunk of N itself, read MN-major (no transposed copy);
+      // one instruction takes 16 negatives = two 8-row groups of 1024 B
       auto gemm2 = [&](int lc) {  // lc: chunk index within this CTA's range
-        const int b = lc & 1;
+        const int b = lc & 1, st = lc % NST;
         if (!mbar_wait(B(C_FULL + b), (lc >> 1) & 1, &err)) return false;
-        if (!mbar_wait(B(FULL_T + b), (lc >> 1) & 1, &err)) return false;
         tc_fence_after();
         const uint32_t cbase = smem_u32(sC_ptr[b]);
         for (int k = 0; k < kChunk / 16; ++k)
-          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc(sT(b) + k * 32), idesc2, (lc > 0 || k > 0) ? 1u : 0u);
+          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc_mn(sN(st) + k * 2048, kChunk * 128, 1024), idesc2,
+               (lc > 0 || k > 0) ? 1u : 0u);
         umma_commit(B(C_FREE + b));
-        umma_commit(B(FREE_T + b));
+        umma_commit(B(FREE_N + st));
         return true;
       };
       for (int lc = 0; ok && lc < nloc; ++lc) {
-        const int b = lc & 1;
-        ok = mbar_wait(B(FULL_N + b), (lc >> 1) & 1, &err);
+        const int b = lc & 1, st = lc % NST;
+        ok = mbar_wait(B(FULL_N + st), (lc / NST) & 1, &err);
         if (ok && lc >= 2) ok = mbar_wait(B(S_FREE + b), ((lc >> 1) + 1) & 1, &err);
         if (!ok) break;
         tc_fence_after();
         const uint32_t tmem_s = tmem + uint32_t(b * kChunk);
         for (int ka = 0; ka < L::kAtoms; ++ka)
           for (int k = 0; k < 4; ++k)
-            umma(tmem_s, umma_desc(sX + ka * kTileRows * 128 + k * 32), umma_desc(sN(b) + ka * kChunk * 128 + k * 32),
+            umma(tmem_s, umma_desc(sX + ka * kTileRows * 128 + k * 32), umma_desc(sN(st) + ka * kChunk * 128 + k * 32),
                  idesc1, (ka | k) ? 1u : 0u);
-        umma_commit(B(FREE_N + b));
         umma_commit(B(S_FULL + b));
         if (lc >= 1) ok = gemm2(lc - 1);
       }
@@ -497,12 +520,17 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const float lr = a.lr[epoch];
     auto epi_sync = []() { asm volatile("bar.sync 1, 256;" ::: "memory"); };
 
-    // |x|^2 of the row from its BF16 values, each half summing half the dims
+    // |x|^2 of the row from its BF16 values in the X tile (the TMA copy of the
+    // rows, 128-byte swizzled atoms), each half summing half the dims in order
     float xx = 0.f;
-    if (row_valid) {
-      const uint4 *xr = reinterpret_cast<const uint4 *>(a.xb + size_t(row_global) * D + hf * (D / 2));
+    const bool x_ok = __all_sync(kFull, mbar_wait(B(FULL_X), 0, &err));
+    if (row_valid && x_ok) {
+      const unsigned char *xrow = sm + L::offX + (t >> 3) * 1024 + (t & 7) * 128;
+#pragma unroll
       for (int i = 0; i < D / 16; ++i) {
-        uint4 u = __ldg(xr + i);
+        const int chunk = hf * (D / 16) + i;  // 16-byte chunk of the row: dims 8 chunk .. 8 chunk + 7
+        const uint4 u = *reinterpret_cast<const uint4 *>(xrow + (chunk >> 3) * (kTileRows * 128) +
+                                                         (((chunk & 7) ^ (t & 7)) << 4));
         const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
         for (int q = 0; q < 4; ++q) {
           float2 f = __bfloat1622float2(h[q]);
@@ -520,6 +548,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const int32_t *nid_loc = a.nid + c_begin * kChunk;
     uint32_t *near_loc = a.near_bits + size_t(row_local) * kNearWords + c_begin * 2 + hf;
     const int et = hf * 128 + t;  // 0..255
+    pdl_wait();  // |n|^2 and ids come from bf16_gather_kernel
     if (et < kChunk)
       negmeta[0][et] = make_float2(__ldg(nn_loc + et), __int_as_float(__ldg(nid_loc + et)));
     epi_sync();
@@ -638,6 +667,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     // Repulsive force rowsum * x - F of every tile row, staged as FP32 rows; x
     // comes from the swizzled X tile.  Thread (row t, half hf) writes dims
     // [hf D/2, (hf+1) D/2).
+    float *const dst_row = stage + t * kPitch;
     for (int d0 = 0; done && d0 < D / 2; d0 += 32) {
       const int dg = hf * (D / 2) + d0;  // first dim of this group of 32
       uint32_t f[32];
@@ -645,69 +675,92 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       tmem_wait_ld();
       const unsigned char *xrow = sm + L::offX + (dg >> 6) * (kTileRows * 128) + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
-      for (int d = 0; d < 32; d += 8) {
+      for (int d = 0; d < 32; d += 4) {
         const int chunk = ((dg & 63) + d) >> 3;  // 16-byte chunk within the 128-byte row
-        const uint4 xu = *reinterpret_cast<const uint4 *>(xrow + ((chunk ^ (t & 7)) << 4));
-        const __nv_bfloat162 *xh = reinterpret_cast<const __nv_bfloat162 *>(&xu);
-        float g[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float2 xv = __bfloat1622float2(xh[q]);
-          g[2 * q] = rowsum * xv.x - __uint_as_float(f[d + 2 * q]);
-          g[2 * q + 1] = rowsum * xv.y - __uint_as_float(f[d + 2 * q + 1]);
-        }
-        float *dst = stage + t * kPitch + dg + d;
-        *reinterpret_cast<float4 *>(dst) = make_float4(g[0], g[1], g[2], g[3]);
-        *reinterpret_cast<float4 *>(dst + 4) = make_float4(g[4], g[5], g[6], g[7]);
+        const uint2 xu = *reinterpret_cast<const uint2 *>(xrow + ((chunk ^ (t & 7)) << 4) + (d & 4) * 2);
+        const float2 x0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xu.x));
+        const float2 x1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xu.y));
+        *reinterpret_cast<float4 *>(dst_row + dg + d) =
+            make_float4(rowsum * x0.x - __uint_as_float(f[d]), rowsum * x0.y - __uint_as_float(f[d + 1]),
+                        rowsum * x1.x - __uint_as_float(f[d + 2]), rowsum * x1.y - __uint_as_float(f[d + 3]));
       }
     }
     if (hf == 0) {
       row_flags[t] = (row_valid && done) ? 1 : 0;
       if (KS == 2) row_loss[t] = loss;
     }
-    epi_sync();
+    if constexpr (KS == 2) {
+      // the staged rows are read next by the bulk copy engine (async proxy)
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      epi_sync();
+      asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+      if (tid == 0) {
+        // this CTA's X tile is free and its INCOMING barrier expects the rows:
+        // tell the peer (a release arrive on the peer's PEER_FREE barrier)
+        mbar_expect_tx(B(INCOMING), kInBytes);
+        mbar_arrive_remote(peer_addr(B(PEER_FREE), peer));
+      }
+      // warp 0 pushes the partials of the peer's 64 rows, their flags and
+      // losses into the peer's X tile once the peer's X tile is free,
+      // completing on the peer's INCOMING barrier
+      if (warp == 0 && __all_sync(kFull, mbar_wait_cluster(B(PEER_FREE), 0, &err))) {
+        const int pr0 = peer * 64;
+        const uint32_t pbar = peer_addr(B(INCOMING), peer);
+        const uint32_t in_base = peer_addr(smem_u32(sm + L::offX), peer);
+        for (int i = lane; i < 64; i += 32)
+          bulk_s2peer(in_base + uint32_t(i * D * 4), smem_u32(stage + (pr0 + i) * kPitch), D * 4, pbar);
+        if (lane == 0) {
+          bulk_s2peer(peer_addr(smem_u32(in_flags), peer), smem_u32(&row_flags[pr0]), 64 * 4, pbar);
+          bulk_s2peer(peer_addr(smem_u32(in_loss), peer), smem_u32(&row_loss[pr0]), 64 * 8, pbar);
+        }
+      }
+    } else {
+      epi_sync();
+    }
 
-    // Coalesced store of lr * force, one warp per row, each lane D/32 consecutive
-    // dims, into rbuf; bf16_apply_kernel adds it to the row together with the
-    // attractive update (which runs concurrently into abuf).
+    // Coalesced store of lr * force, one warp per row, lane l the 16-byte
+    // vectors l, l + 32, ... (every store instruction writes whole 32-byte
+    // sectors), into rbuf; bf16_apply_kernel adds it to the row together with
+    // the attractive update (which runs concurrently into abuf).
     for (int rr = warp; KS == 1 && rr < kTileRows; rr += kEpiThreads / 32) {
       if (row_flags[rr] == 0) continue;
-      const int rl = tile_base + rr;
-      const float *src = stage + rr * kPitch + lane * kPer;
-      float *rbp = a.rbuf + size_t(rl) * D + lane * kPer;
+      const float4 *src = reinterpret_cast<const float4 *>(stage + rr * kPitch);
+      float4 *rbp = reinterpret_cast<float4 *>(a.rbuf + size_t(tile_base + rr) * D);
 #pragma unroll
-      for (int q = 0; q < kPer; q += 2) {
-        const float2 f2 = *reinterpret_cast<const float2 *>(src + q);
-        *reinterpret_cast<float2 *>(rbp + q) = make_float2(lr * f2.x, lr * f2.y);
+      for (int v = lane; v < D / 4; v += 32) {
+        const float4 f = src[v];
+        rbp[v] = make_float4(lr * f.x, lr * f.y, lr * f.z, lr * f.w);
       }
+    }
+    if constexpr (KS == 2) {
+      // this CTA's rows [64 ks, 64 ks + 64): own partial + the peer's
+      const bool in_ok = __all_sync(kFull, mbar_wait_cluster(B(INCOMING), 0, &err));
+      // the peer's copies into this CTA have landed, so the peer's staged rows
+      // are no longer read: tell the peer at once
+      if (tid == 0 && in_ok) mbar_arrive_remote(peer_addr(B(PEER_GOT), peer));
+      const float *in_rows = reinterpret_cast<const float *>(sm + L::offX);
+      const int r0 = ks * 64;
+      for (int i = warp; in_ok && i < 64; i += kEpiThreads / 32) {
+        if (row_flags[r0 + i] == 0 || in_flags[i] == 0) continue;
+        const float4 *own = reinterpret_cast<const float4 *>(stage + (r0 + i) * kPitch);
+        const float4 *oth = reinterpret_cast<const float4 *>(in_rows + i * D);
+        float4 *rbp = reinterpret_cast<float4 *>(a.rbuf + size_t(tile_base + r0 + i) * D);
+#pragma unroll
+        for (int v = lane; v < D / 4; v += 32) {
+          const float4 p = own[v], q = oth[v];
+          rbp[v] = make_float4(lr * (p.x + q.x), lr * (p.y + q.y), lr * (p.z + q.z), lr * (p.w + q.w));
+        }
+      }
+      if (in_ok && tid < 64 && row_flags[r0 + tid] != 0 && in_flags[tid] != 0)
+        a.loss_row[a.base + tile_base + r0 + tid] = row_loss[r0 + tid] + in_loss[tid];
+      // the CTA (and its shared memory) ends only after the peer has received
+      // this CTA's rows
+      if (tid == 0) mbar_wait_cluster(B(PEER_GOT), 0, &err);
     }
   }
   if constexpr (KS == 2) {
     __syncwarp();
-    cluster_barrier();  // both CTAs' staged rows, flags and losses are complete
-    if (warp < kEpiThreads / 32) {
-      const int peer = ks ^ 1;
-      const float lr = a.lr[a.epoch[0]];
-      constexpr int kHalf = kTileRows / 2;
-      for (int rr = ks * kHalf + warp; rr < (ks + 1) * kHalf; rr += kEpiThreads / 32) {
-        if (row_flags[rr] == 0) continue;
-        const float *src = stage + rr * kPitch + lane * kPer;
-        const uint32_t psrc = peer_addr(smem_u32(src), peer);
-        float *rbp = a.rbuf + size_t(tile_base + rr) * D + lane * kPer;
-#pragma unroll
-        for (int q = 0; q < kPer; q += 2) {
-          const float2 own = *reinterpret_cast<const float2 *>(src + q);
-          const float2 oth = ld_peer_f2(psrc + 4u * uint32_t(q));
-          *reinterpret_cast<float2 *>(rbp + q) = make_float2(lr * (own.x + oth.x), lr * (own.y + oth.y));
-        }
-      }
-      if (tid < kHalf) {
-        const int rr = ks * kHalf + tid;
-        if (row_flags[rr] != 0)
-          a.loss_row[a.base + tile_base + rr] = row_loss[rr] + ld_peer_f64(peer_addr(smem_u32(&row_loss[rr]), peer));
-      }
-    }
-    cluster_barrier();  // the peer has finished reading this CTA's shared memory
+    if (warp >= kEpiThreads / 32) asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
@@ -910,54 +963,95 @@ namespace {
 
 // The repulsion GEMMs of a minibatch: one CTA per 128-row tile, or, with at
 // least two chunks of negatives, a cluster of two CTAs per tile that split them.
+// pdl: a programmatic dependency on the gather launched just before on s (the
+// prologue overlaps it); prio: the launch's scheduling priority (0: none).
 template <int D>
-cudaError_t launch_repulse(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                           const CUtensorMap &mt, int tiles, cudaStream_t s) {
-  if (a.kpad / kChunk < 2) {
-    bf16_repulse_kernel<D, 1><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s>>>(mx, mn, mt, a);
-    return cudaGetLastError();
-  }
+cudaError_t launch_repulse(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn, int tiles,
+                           cudaStream_t s, bool pdl, int prio) {
+  const bool split = a.kpad / kChunk >= 2;
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(2 * tiles);
+  cfg.gridDim = dim3(split ? 2 * tiles : tiles);
   cfg.blockDim = dim3(kRepulseThreads);
   cfg.dynamicSmemBytes = RepulseSmem<D>::dynamic;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
+  cudaLaunchAttribute attr[3];
+  int na = 0;
+  if (split) {
+    attr[na].id = cudaLaunchAttributeClusterDimension;
+    attr[na].val.clusterDim.x = 2;
+    attr[na].val.clusterDim.y = 1;
+    attr[na].val.clusterDim.z = 1;
+    ++na;
+  }
+  if (pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  if (prio) {
+    attr[na].id = cudaLaunchAttributePriority;
+    attr[na].val.priority = prio;
+    ++na;
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 2>, mx, mn, mt, a);
+  cfg.numAttrs = na;
+  return split ? cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 2>, mx, mn, a)
+               : cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 1>, mx, mn, a);
+}
+
+// The gather of the negatives (at priority prio, 0: none).
+template <int D>
+cudaError_t launch_gather(const BF16BatchArgs &a, cudaStream_t s, int prio) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(a.kpad / kGatherTile);  // kpad: a multiple of 64
+  cfg.blockDim = dim3(kGatherTile * 32);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = prio;
+  cfg.attrs = attr;
+  cfg.numAttrs = prio ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, bf16_gather_kernel<D>, a);
+}
+
+// The highest scheduling priority of the device (numerically the least).
+int top_priority() {
+  static const int prio = [] {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+    return greatest;
+  }();
+  return prio;
 }
 
 template <int D, int U>
 cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                                const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                                cudaEvent_t fork, cudaEvent_t join) {
+                                cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                                cudaEvent_t fork, cudaEvent_t join, bool pdl) {
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
-  const int gather_ctas = a.kpad / kGatherTile;  // kpad: a multiple of 64
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
   const int apply_ctas = (a.rows + 7) / 8;
   cudaError_t e = cudaSuccess;
   if (ev || !s2) {  // one after another (per-kernel timing)
     if (ev) cudaEventRecord(ev[0], s);
-    bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s>>>(a);
+    if ((e = launch_gather<D>(a, s, 0)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[1], s);
     bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
-    if ((e = launch_repulse<D>(a, mx, mn, mt, tiles, s)) != cudaSuccess) return e;
+    if ((e = launch_repulse<D>(a, mx, mn, tiles, s, false, 0)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[3], s);
     bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
     return cudaGetLastError();
   }
   // the attractive pass and the negatives' path (gather, repulsion GEMMs) are
   // independent within a minibatch: they run on two streams, forked after the
-  // previous minibatch's update and joined before this one's
+  // previous minibatch's update and joined before this one's.  The negatives'
+  // path is launched first and at the top priority, so the GEMM CTAs (one SM
+  // each) are placed before the attractive pass fills the SMs; the GEMMs'
+  // prologue overlaps the gather (programmatic dependency)
   if ((e = cudaEventRecord(fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(s2, fork, 0)) != cudaSuccess) return e;
-  bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s2>>>(a);
-  if ((e = launch_repulse<D>(a, mx, mn, mt, tiles, s2)) != cudaSuccess) return e;
+  if ((e = launch_gather<D>(a, s2, top_priority())) != cudaSuccess) return e;
+  if ((e = launch_repulse<D>(a, mx, mn, tiles, s2, pdl, top_priority())) != cudaSuccess) return e;
   bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
   if ((e = cudaEventRecord(join, s2)) != cudaSuccess || (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
   bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
@@ -967,12 +1061,12 @@ cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, c
 }  // namespace
 
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                              cudaEvent_t fork, cudaEvent_t join) {
+                              cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                              cudaEvent_t fork, cudaEvent_t join, bool pdl) {
   switch (dim) {
-    case 64: return launch_bf16_batch_d<64, 8>(a, mx, mn, mt, s, ev, s2, fork, join);
-    case 128: return launch_bf16_batch_d<128, 8>(a, mx, mn, mt, s, ev, s2, fork, join);
-    case 256: return launch_bf16_batch_d<256, 4>(a, mx, mn, mt, s, ev, s2, fork, join);
+    case 64: return launch_bf16_batch_d<64, 8>(a, mx, mn, s, ev, s2, fork, join, pdl);
+    case 128: return launch_bf16_batch_d<128, 8>(a, mx, mn, s, ev, s2, fork, join, pdl);
+    case 256: return launch_bf16_batch_d<256, 4>(a, mx, mn, s, ev, s2, fork, join, pdl);
   }
   return cudaErrorInvalidValue;
 }

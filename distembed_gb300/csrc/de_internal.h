@@ -135,7 +135,6 @@ struct BF16BatchArgs {
   float *abuf;              // [B, dim] attractive update of the minibatch (lr applied)
   float *rbuf;              // [B, dim] repulsive (GEMM) update of the minibatch (lr applied)
   __nv_bfloat16 *nb;        // [kpad, dim] gathered negatives
-  __nv_bfloat16 *nbt;       // [dim, kpad] the same, transposed
   float *nn;                // [kpad] squared norms of the gathered negatives
   int32_t *nid;             // [kpad] vertex id of each negative, -1 = none
   uint32_t *near_bits;      // [B, kpad / 32] bit k: pair (row, negative k) takes the exact
@@ -164,10 +163,11 @@ cudaError_t bf16_prepare(int dim);
 // repulsion GEMMs (on s2, forked and joined with the two events), then the
 // update with the exact close pairs.  ev (nullable): four events recorded before
 // the gather, attractive, GEMM and update launches, all on s one after another
-// (so is everything when s2 is null).
+// (so is everything when s2 is null).  pdl: on s2 the GEMMs depend on the
+// gather programmatically (their prologue overlaps it).
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
-                              const CUtensorMap &mt, cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                              cudaEvent_t fork, cudaEvent_t join);
+                              cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
+                              cudaEvent_t fork, cudaEvent_t join, bool pdl);
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
 cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
 

@@ -109,7 +109,7 @@ struct de_handle {
   size_t rbuf_cap = 0;
   cudaStream_t stream2 = nullptr;  // the repulsion GEMMs, forked from and joined to `stream`
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  __nv_bfloat16 *d_nb = nullptr, *d_nbt = nullptr;
+  __nv_bfloat16 *d_nb = nullptr;
   size_t nb_cap = 0;
   float *d_nn = nullptr;
   int32_t *d_nid = nullptr;
@@ -119,7 +119,7 @@ struct de_handle {
   double *d_loss_row = nullptr;
   int32_t *d_err = nullptr;
   int kpad = 0;
-  CUtensorMap map_x{}, map_n{}, map_t{};
+  CUtensorMap map_x{}, map_n{};
 
   // where device and host buffers come from (default: cudaMalloc / cudaHostAlloc)
   MemHooks hooks{};
@@ -345,7 +345,6 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.abuf = h->d_abuf;
     a.rbuf = h->d_rbuf;
     a.nb = h->d_nb;
-    a.nbt = h->d_nbt;
     a.nn = h->d_nn;
     a.nid = h->d_nid;
     a.near_bits = h->d_near_bits;
@@ -353,8 +352,8 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.loss_off = s.item_off[j];
     a.loss_row = h->d_loss_row;
     a.err = h->d_err;
-    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, h->map_t, st, ev ? ev + 4 * j : nullptr, h->stream2,
-                            h->ev_fork, h->ev_join);
+    err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, st, ev ? ev + 4 * j : nullptr, h->stream2,
+                            h->ev_fork, h->ev_join, h->opt.pdl != 0);
   }
   if (err == cudaSuccess) {
     BF16FlushArgs f{};
@@ -389,22 +388,19 @@ int ensure_bf16_buffers(de_handle *h, int ns, bool *moved) {
     m = true;
   }
   if (size_t(kpad) > h->kpad_cap || !h->d_nn) {
-    for (void *p : {static_cast<void *>(h->d_nn), static_cast<void *>(h->d_nid), static_cast<void *>(h->d_nb),
-                    static_cast<void *>(h->d_nbt)})
+    for (void *p : {static_cast<void *>(h->d_nn), static_cast<void *>(h->d_nid), static_cast<void *>(h->d_nb)})
       if (p) dev_free(h, p);
-    h->d_nn = nullptr; h->d_nid = nullptr; h->d_nb = nullptr; h->d_nbt = nullptr;
+    h->d_nn = nullptr; h->d_nid = nullptr; h->d_nb = nullptr;
     DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nn), kpad * sizeof(float)));
     DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nid), kpad * sizeof(int32_t)));
     DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nb), size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
-    DE_CUDA(h, dev_alloc(h, reinterpret_cast<void **>(&h->d_nbt), size_t(kpad) * h->dim * sizeof(__nv_bfloat16)));
     h->kpad_cap = kpad;
     m = true;
   }
   if (kpad != h->kpad || m) {
     h->kpad = kpad;
     if ((rc = encode_map(h, &h->map_x, h->d_xb, uint64_t(h->n), uint64_t(h->dim), 128)) ||
-        (rc = encode_map(h, &h->map_n, h->d_nb, uint64_t(kpad), uint64_t(h->dim), 64)) ||
-        (rc = encode_map(h, &h->map_t, h->d_nbt, uint64_t(h->dim), uint64_t(kpad), uint32_t(h->dim))))
+        (rc = encode_map(h, &h->map_n, h->d_nb, uint64_t(kpad), uint64_t(h->dim), 64)))
       return rc;
     m = true;
   }
@@ -678,7 +674,6 @@ int de_destroy(de_handle *h) {
   dev_free(h, h->d_abuf);
   dev_free(h, h->d_rbuf);
   dev_free(h, h->d_nb);
-  dev_free(h, h->d_nbt);
   dev_free(h, h->d_nn);
   dev_free(h, h->d_nid);
   dev_free(h, h->d_near_bits);
