@@ -255,10 +255,12 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       : "memory");
 }
 
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+// One tcgen05 MMA (BF16 x BF16 -> FP32 in tensor memory) with A in tensor memory
+// (M lanes, K packed two BF16 per column) and B from a shared-memory descriptor.
+__device__ __forceinline__ void umma_ta(uint32_t tmem_d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t accumulate) {
   asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -278,7 +280,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 16 consecutive columns of this warp's 32 lanes from registers.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -288,14 +309,15 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 template <int D>
 struct RepulseSmem {
   static constexpr int kAtoms = D / 64;                  // 128-B column atoms of a dim-wide row
-  static constexpr int kStages = 4;                      // chunks of N in flight
+  static constexpr int kStages = 6;                      // chunks of N in flight
   static constexpr int kX = kAtoms * kTileRows * 128;    // X tile
-  static constexpr int kN = kAtoms * kChunk * 128;       // one chunk of N (operand of both GEMMs)
-  static constexpr int kC = kTileRows * 128;             // one chunk of C (128 rows x 64 coefficients)
-  static constexpr int offX = 0;
-  static constexpr int offN = offX + kX;
-  static constexpr int offC = offN + kStages * kN;
-  static constexpr int bytes = offC + 2 * kC;
+  static constexpr int kN = kAtoms * kChunk * 128;       // one chunk of N (B operand of both GEMMs)
+  static_assert(kX == 2 * kN, "the X tile takes two stages");
+  static constexpr int kMisc = 16384;                    // per-row exchanges, flags and losses
+  static constexpr int offN = 0;
+  static constexpr int offX = offN + (kStages - 2) * kN;  // first over the last two stages
+  static constexpr int offMisc = offN + kStages * kN;
+  static constexpr int bytes = offMisc + kMisc;
   static constexpr int dynamic = bytes + 1024;           // + alignment slack
 };
 
@@ -303,9 +325,15 @@ struct RepulseSmem {
 // Epilogue warp w serves TMEM lane quadrant w % 4 (tile rows 32(w%4) .. +31) and
 // column half w / 4: 32 of the 64 coefficients of each chunk, and half of the
 // dims in the final update.  TMEM: S chunks in columns [0, 128) (double
-// buffered), F in columns [256, 256 + dim).  Chunks of N stream through a ring
-// of four shared-memory stages; each stage is the B operand of both GEMMs (K-
-// major for S = X N^T, MN-major for F += C N), so no transposed copy exists.
+// buffered; the epilogue overwrites a chunk's S with its BF16 coefficients C,
+// packed two per column, which the second GEMM reads as its A operand), the
+// BF16 X tile in columns [128, 128 + dim / 2) (the first GEMM's A operand,
+// written once by the epilogue warps from the TMA copy), F in columns
+// [256, 256 + dim).  Both A operands live in tensor memory, so the shared-memory
+// traffic of a chunk is its N (the B operand of both GEMMs: K-major for
+// S = X N^T, MN-major for F += C N, so no transposed copy exists) streaming
+// through a ring of six stages, the last two of which first hold the TMA copy
+// of the X tile (until it is in tensor memory).
 //
 // KS = 2: the negatives of a tile are split between the two CTAs of a cluster
 // (rank 0: the first ceil(chunks / 2) chunks, rank 1 the rest), so twice as
@@ -327,6 +355,25 @@ __device__ __forceinline__ int cta_rank_in_cluster() {
 // Release arrive on a barrier of the peer CTA (address from peer_addr).
 __device__ __forceinline__ void mbar_arrive_remote(uint32_t bar) {
   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// mbar_wait for threads that may wait long and share their SM sub-partition
+// with the MMA-issuing thread: each poll may suspend the thread (up to 2 us,
+// woken early when the phase completes) instead of spinning on the issue slots;
+// bounded like mbar_wait.
+constexpr long kSleepPolls = 1L << 20;
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, int *err_shared) {
+  for (long it = 0; it < kSleepPolls; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(2000)
+        : "memory");
+    if (ok) return true;
+    if (*reinterpret_cast<volatile int *>(err_shared)) return false;
+  }
+  *reinterpret_cast<volatile int *>(err_shared) = 1;
+  return false;
 }
 // mbar_wait with cluster-scope acquire (the phase was completed by the peer CTA).
 __device__ __forceinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity, int *err_shared) {
@@ -364,7 +411,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   using L = RepulseSmem<D>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ __align__(8) uint64_t bar[21];
+  __shared__ __align__(8) uint64_t bar[24];
   __shared__ uint32_t tmem_holder;
   __shared__ int err;
   __shared__ float2 negmeta[2][kChunk];  // (|n|^2, vertex id) of a chunk's negatives
@@ -377,15 +424,22 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   const int c_begin = ks == 0 ? 0 : (nchunks + 1) / 2;
   const int c_end = (KS == 1 || ks == 1) ? nchunks : (nchunks + 1) / 2;
   const int nloc = c_end - c_begin;
+  // Step lc of this CTA takes its chunk cl(lc) = (lc + rot) mod nloc: tiles
+  // start at different chunks, so at any moment the CTAs fetch different parts
+  // of N from L2 instead of all the same 32 KB (F and the loss sum the chunks in
+  // this order).
+  const int rot = (blockIdx.x / KS) % nloc;
+  auto cl = [&](int lc) { return lc + rot < nloc ? lc + rot : lc + rot - nloc; };
 
   // barrier ids
   constexpr int NST = L::kStages;
   const uint32_t b0 = smem_u32(&bar[0]);
   auto B = [&](int i) { return b0 + 8u * uint32_t(i); };
-  const int FULL_X = 0, FULL_N = 1, FREE_N = FULL_N + NST, S_FULL = FREE_N + NST, S_FREE = S_FULL + 2,
-            C_FULL = S_FREE + 2, C_FREE = C_FULL + 2, F_DONE = C_FREE + 2, INCOMING = F_DONE + 1,
-            PEER_FREE = INCOMING + 1, PEER_GOT = PEER_FREE + 1;
-  static_assert(1 + 2 * NST + 8 + 4 <= 21, "barrier slots");
+  const int FULL_X = 0, FULL_N = 1, FREE_N = FULL_N + NST, X_TMEM = FREE_N + NST, S_FULL = X_TMEM + 1,
+            C_FULL = S_FULL + 2, F_DONE = C_FULL + 2, INCOMING = F_DONE + 1, PEER_FREE = INCOMING + 1,
+            PEER_GOT = PEER_FREE + 1;
+  static_assert(1 + 2 * NST + 1 + 4 + 4 <= 24, "barrier slots");
+  constexpr uint32_t kColX = 128, kColF = 256;  // tensor-memory columns of X and F
   auto failed = [&]() { return *reinterpret_cast<volatile int *>(&err) != 0; };
 
   if (tid == 0) {
@@ -395,11 +449,10 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       mbar_init(B(FULL_N + i), 1);
       mbar_init(B(FREE_N + i), 1);
     }
+    mbar_init(B(X_TMEM), kEpiThreads);
     for (int i = 0; i < 2; ++i) {
       mbar_init(B(S_FULL + i), 1);
-      mbar_init(B(S_FREE + i), kEpiThreads);
       mbar_init(B(C_FULL + i), kEpiThreads);
-      mbar_init(B(C_FREE + i), 1);
     }
     mbar_init(B(F_DONE), 1);
     mbar_init(B(INCOMING), 1);
@@ -422,21 +475,27 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   const uint32_t tmem = tmem_holder;
   const uint32_t sX = smem_u32(sm + L::offX);
   auto sN = [&](int st) { return smem_u32(sm + L::offN + st * L::kN); };
-  unsigned char *sC_ptr[2] = {sm + L::offC, sm + L::offC + L::kC};
-  // after the GEMMs: the staged force rows (pitch D + 4 floats) over the operand
-  // buffers (at dim 256 reaching into C[0]); per tile row a flag (nonzero: the
-  // row's force is final) and, with KS = 2, its loss, both in C[1]
+  // the misc area: per-row exchanges between the two column halves ([0, 4096),
+  // used before the staging), then per tile row a flag (nonzero: the row's
+  // force is final) and, with KS = 2, its loss, then the peer's flags and losses
+  unsigned char *const misc = sm + L::offMisc;
+  float *const xx_part = reinterpret_cast<float *>(misc);
+  float *const rs_part = reinterpret_cast<float *>(misc + 1024);
+  double *const loss_part = reinterpret_cast<double *>(misc + 2048);
+  int *const row_flags = reinterpret_cast<int *>(misc + 4096);
+  double *const row_loss = reinterpret_cast<double *>(misc + 5120);
+  int *const in_flags = reinterpret_cast<int *>(misc + 8192);
+  double *const in_loss = reinterpret_cast<double *>(misc + 8448);
+  // after the GEMMs: the staged force rows (pitch D + 4 floats) over the N
+  // stages; KS = 2: after them the peer's partials of this CTA's 64 rows (pitch
+  // D floats, reaching 2048 B into the then dead half-row exchange area), their
+  // 64 flags and 64 losses in the misc area
   constexpr int kPitch = D + 4;
+  constexpr int kStageBytes = kTileRows * kPitch * 4;
   float *const stage = reinterpret_cast<float *>(sm + L::offN);
-  // KS = 2: the peer's partials of this CTA's 64 rows arrive in the X tile
-  // (pitch D floats), their 64 flags and 64 losses in C[1] after the own ones
-  static_assert(64 * D * 4 == L::kX, "the incoming rows fill the X tile");
-  int *const in_flags = reinterpret_cast<int *>(sC_ptr[1] + 4096);
-  double *const in_loss = reinterpret_cast<double *>(sC_ptr[1] + 8192);
+  float *const in_rows = reinterpret_cast<float *>(sm + L::offN + kStageBytes);
+  static_assert(kStageBytes + 64 * D * 4 <= L::offMisc - L::offN + 2048, "incoming rows end before loss_part");
   constexpr uint32_t kInBytes = 64 * D * 4 + 64 * 4 + 64 * 8;
-  static_assert(kTileRows * kPitch * 4 <= NST * L::kN + L::kC, "staging fits before C[1]");
-  int *const row_flags = reinterpret_cast<int *>(sC_ptr[1]);
-  double *const row_loss = reinterpret_cast<double *>(sC_ptr[1] + 1024);
 
   if (warp == 8) {
     // ---------------- TMA producer
@@ -449,10 +508,15 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       // running under a programmatic dependency): wait for it
       pdl_wait();
       // chunk lc into stage lc % NST once the second GEMM of chunk lc - NST has
-      // read that stage
+      // read that stage; the last two stages are first free once the epilogue
+      // warps have copied the X tile into tensor memory
       for (int lc = 0; lc < nloc && !failed(); ++lc) {
-        const int c = c_begin + lc, st = lc % NST, use = lc / NST;
-        if (use > 0 && !mbar_wait(B(FREE_N + st), (use - 1) & 1, &err)) break;
+        const int c = c_begin + cl(lc), st = lc % NST, use = lc / NST;
+        if (use > 0) {
+          if (!mbar_wait_sleep(B(FREE_N + st), (use - 1) & 1, &err)) break;
+        } else if (st >= NST - 2) {
+          if (!mbar_wait_sleep(B(X_TMEM), 0, &err)) break;
+        }
         mbar_expect_tx(B(FULL_N + st), L::kN);
         for (int ka = 0; ka < L::kAtoms; ++ka)
           tma_load_2d(sN(st) + ka * kChunk * 128, &map_n, ka * 64, c * kChunk, B(FULL_N + st));
@@ -471,33 +535,38 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     if (lane == 0) {
       constexpr uint32_t idesc1 = umma_idesc(kTileRows, kChunk);
       constexpr uint32_t idesc2 = umma_idesc(kTileRows, D, true);
-      const uint32_t tmem_f = tmem + 256;
-      bool ok = mbar_wait(B(FULL_X), 0, &err);
-      // F += C N: B is the chunk of N itself, read MN-major (no transposed copy);
-      // one instruction takes 16 negatives = two 8-row groups of 1024 B
+      const uint32_t tmem_f = tmem + kColF;
+      bool ok = mbar_wait(B(X_TMEM), 0, &err);  // X in tensor memory (stored by the epilogue warps)
+      // F += C N: A = the chunk's coefficients in tensor memory (over its S), B =
+      // the chunk of N itself, read MN-major; one instruction takes 16 negatives
+      // (8 columns of C, two 8-row groups of 1024 B of N)
       auto gemm2 = [&](int lc) {  // lc: chunk index within this CTA's range
         const int b = lc & 1, st = lc % NST;
         if (!mbar_wait(B(C_FULL + b), (lc >> 1) & 1, &err)) return false;
         tc_fence_after();
-        const uint32_t cbase = smem_u32(sC_ptr[b]);
-        for (int k = 0; k < kChunk / 16; ++k)
-          umma(tmem_f, umma_desc(cbase + k * 32), umma_desc_mn(sN(st) + k * 2048, kChunk * 128, 1024), idesc2,
-               (lc > 0 || k > 0) ? 1u : 0u);
-        umma_commit(B(C_FREE + b));
+        const uint64_t dn = umma_desc_mn(sN(st), kChunk * 128, 1024);
+#pragma unroll
+        for (int k = 0; k < kChunk / 16; ++k)  // descriptor address fields step by bytes / 16
+          umma_ta(tmem_f, tmem + uint32_t(b * kChunk + 8 * k), dn + uint64_t(k * 2048 / 16), idesc2,
+                  (lc > 0 || k > 0) ? 1u : 0u);
         umma_commit(B(FREE_N + st));
         return true;
       };
       for (int lc = 0; ok && lc < nloc; ++lc) {
         const int b = lc & 1, st = lc % NST;
+        // S buffer b last held the coefficients of chunk lc - 2, read by that
+        // chunk's second GEMM, which this thread issued before this first GEMM:
+        // tcgen05.mma instructions of one thread are performed in issue order,
+        // so no wait is needed before overwriting it
         ok = mbar_wait(B(FULL_N + st), (lc / NST) & 1, &err);
-        if (ok && lc >= 2) ok = mbar_wait(B(S_FREE + b), ((lc >> 1) + 1) & 1, &err);
         if (!ok) break;
         tc_fence_after();
         const uint32_t tmem_s = tmem + uint32_t(b * kChunk);
-        for (int ka = 0; ka < L::kAtoms; ++ka)
-          for (int k = 0; k < 4; ++k)
-            umma(tmem_s, umma_desc(sX + ka * kTileRows * 128 + k * 32), umma_desc(sN(st) + ka * kChunk * 128 + k * 32),
-                 idesc1, (ka | k) ? 1u : 0u);
+        const uint64_t dn = umma_desc(sN(st));
+#pragma unroll
+        for (int kk = 0; kk < D / 16; ++kk)  // 16 dims per step: 8 columns of X, 32 B of an N atom row
+          umma_ta(tmem_s, tmem + kColX + uint32_t(8 * kk),
+                  dn + uint64_t(((kk >> 2) * kChunk * 128 + (kk & 3) * 32) / 16), idesc1, kk ? 1u : 0u);
         umma_commit(B(S_FULL + b));
         if (lc >= 1) ok = gemm2(lc - 1);
       }
@@ -520,27 +589,40 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const float lr = a.lr[epoch];
     auto epi_sync = []() { asm volatile("bar.sync 1, 256;" ::: "memory"); };
 
-    // |x|^2 of the row from its BF16 values in the X tile (the TMA copy of the
-    // rows, 128-byte swizzled atoms), each half summing half the dims in order
+    const uint32_t lane_base = uint32_t(q4 * 32) << 16;
+    // The row's BF16 values from the X tile (the TMA copy of the rows, 128-byte
+    // swizzled atoms), each half its D/2 dims: into tensor memory as the first
+    // GEMM's A operand (column kColX + j holds dims 2j, 2j+1), and |x|^2 summed
+    // in dim order
     float xx = 0.f;
-    const bool x_ok = __all_sync(kFull, mbar_wait(B(FULL_X), 0, &err));
-    if (row_valid && x_ok) {
+    const bool x_ok = __all_sync(kFull, mbar_wait_sleep(B(FULL_X), 0, &err));
+    {
       const unsigned char *xrow = sm + L::offX + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
-      for (int i = 0; i < D / 16; ++i) {
-        const int chunk = hf * (D / 16) + i;  // 16-byte chunk of the row: dims 8 chunk .. 8 chunk + 7
-        const uint4 u = *reinterpret_cast<const uint4 *>(xrow + (chunk >> 3) * (kTileRows * 128) +
-                                                         (((chunk & 7) ^ (t & 7)) << 4));
-        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
-        for (int q = 0; q < 4; ++q) {
-          float2 f = __bfloat1622float2(h[q]);
-          xx = fmaf(f.x, f.x, fmaf(f.y, f.y, xx));
+      for (int g = 0; g < D / 64; ++g) {  // 16 columns (32 dims) at a time
+        uint32_t w[16];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int chunk = hf * (D / 16) + g * 4 + i;  // 16-byte chunk of the row: dims 8 chunk .. 8 chunk + 7
+          const uint4 u = x_ok ? *reinterpret_cast<const uint4 *>(xrow + (chunk >> 3) * (kTileRows * 128) +
+                                                                  (((chunk & 7) ^ (t & 7)) << 4))
+                               : make_uint4(0u, 0u, 0u, 0u);
+          w[4 * i] = u.x, w[4 * i + 1] = u.y, w[4 * i + 2] = u.z, w[4 * i + 3] = u.w;
+          const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 f = __bfloat1622float2(h[q]);
+            xx = fmaf(f.x, f.x, fmaf(f.y, f.y, xx));
+          }
         }
+        tmem_st16(tmem + lane_base + kColX + uint32_t(hf * (D / 4) + g * 16), w);
       }
+      if (!row_valid) xx = 0.f;
     }
-    // per-row exchange between the two column halves, in the C buffers while
-    // they are idle: before chunk 1 writes C[1], and after every GEMM is done
-    float *xx_part = reinterpret_cast<float *>(sC_ptr[1]);
+    tmem_wait_st();
+    tc_fence_before();
+    mbar_arrive(B(X_TMEM));
+    // per-row exchange between the two column halves
     xx_part[hf * kTileRows + t] = xx;
     // |n|^2 and vertex id of the chunk's negatives, staged once per chunk; this
     // CTA's chunks start at c_begin (metadata, and the row's bitmask words)
@@ -550,33 +632,29 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const int et = hf * 128 + t;  // 0..255
     pdl_wait();  // |n|^2 and ids come from bf16_gather_kernel
     if (et < kChunk)
-      negmeta[0][et] = make_float2(__ldg(nn_loc + et), __int_as_float(__ldg(nid_loc + et)));
+      negmeta[0][et] = make_float2(__ldg(nn_loc + cl(0) * kChunk + et), __int_as_float(__ldg(nid_loc + cl(0) * kChunk + et)));
     epi_sync();
     xx = xx_part[t] + xx_part[kTileRows + t];
 
     float rowsum = 0.f;
     double loss = 0.0;
-    const uint32_t lane_base = uint32_t(q4 * 32) << 16;
     for (int lc = 0; lc < nloc; ++lc) {
       const int b = lc & 1;
-      if (lc > 0) epi_sync();  // meta of chunk c visible; everyone is done with chunk c-1
-      // next chunk's metadata: loads issued now, stored at the end of this chunk
+      // next chunk's metadata: loads issued now, stored before this chunk's barrier
       const bool pre = lc + 1 < nloc && et < kChunk;
       float pre_nn = 0.f;
       int pre_id = -1;
       if (pre) {
-        pre_nn = __ldg(nn_loc + (lc + 1) * kChunk + et);
-        pre_id = __ldg(nid_loc + (lc + 1) * kChunk + et);
+        pre_nn = __ldg(nn_loc + cl(lc + 1) * kChunk + et);
+        pre_id = __ldg(nid_loc + cl(lc + 1) * kChunk + et);
       }
       uint32_t s_raw[32] = {};
-      const bool got = __all_sync(kFull, mbar_wait(B(S_FULL + b), (lc >> 1) & 1, &err));
+      const bool got = __all_sync(kFull, mbar_wait_sleep(B(S_FULL + b), (lc >> 1) & 1, &err));
       tc_fence_after();
       if (got) {
         tmem_ld32(tmem + lane_base + uint32_t(b * kChunk + hf * 32), s_raw);
         tmem_wait_ld();
       }
-      tc_fence_before();
-      mbar_arrive(B(S_FREE + b));
       // Coefficients without branches, so the 32 pairs' chains interleave.  A
       // negative that is no draw (padding, or a draw equal to n) has |n|^2 = +inf,
       // so its r is +inf and its coefficient 0.  A pair with r < kNearR takes the
@@ -639,23 +717,22 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         }
         rowsum += rs2.x + rs2.y;
       }
-      if (near_word) near_loc[lc * 2] = near_word;
-      if (lc >= 2) mbar_wait(B(C_FREE + b), ((lc >> 1) + 1) & 1, &err);
-      unsigned char *crow = sC_ptr[b] + (t >> 3) * 1024 + (t & 7) * 128;
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        *reinterpret_cast<uint4 *>(crow + (((hf * 4 + j) ^ (t & 7)) << 4)) =
-            make_uint4(packed[4 * j], packed[4 * j + 1], packed[4 * j + 2], packed[4 * j + 3]);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(B(C_FULL + b));
+      if (near_word) near_loc[cl(lc) * 2] = near_word;
       if (pre) negmeta[b ^ 1][et] = make_float2(pre_nn, __int_as_float(pre_id));
+      // every thread has read this chunk's S (which C overwrites: the row's other
+      // half reads columns this half writes) and metadata; the next chunk's
+      // metadata is visible after this barrier
+      epi_sync();
+      // C of this half (coefficients hf*32 .. +31, two per column) over S
+      if (got) tmem_st16(tmem + lane_base + uint32_t(b * kChunk + hf * 16), packed);
+      tmem_wait_st();
+      tc_fence_before();
+      mbar_arrive(B(C_FULL + b));
     }
     // every lane of a warp takes the same branch around the (warp-wide) TMEM loads
-    const bool done = __all_sync(kFull, mbar_wait(B(F_DONE), 0, &err) && !failed());
+    const bool done = __all_sync(kFull, mbar_wait_sleep(B(F_DONE), 0, &err) && !failed());
     tc_fence_after();
     // combine the two column halves of each row
-    float *rs_part = reinterpret_cast<float *>(sC_ptr[0]);
-    double *loss_part = reinterpret_cast<double *>(sC_ptr[0] + 1024);
     rs_part[hf * kTileRows + t] = rowsum;
     loss_part[hf * kTileRows + t] = loss;
     epi_sync();
@@ -665,21 +742,19 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     epi_sync();  // the staging below may overwrite the combine area
 
     // Repulsive force rowsum * x - F of every tile row, staged as FP32 rows; x
-    // comes from the swizzled X tile.  Thread (row t, half hf) writes dims
-    // [hf D/2, (hf+1) D/2).
+    // comes from the BF16 X tile in tensor memory.  Thread (row t, half hf)
+    // writes dims [hf D/2, (hf+1) D/2).
     float *const dst_row = stage + t * kPitch;
     for (int d0 = 0; done && d0 < D / 2; d0 += 32) {
       const int dg = hf * (D / 2) + d0;  // first dim of this group of 32
-      uint32_t f[32];
-      tmem_ld32(tmem + lane_base + 256u + uint32_t(dg), f);
+      uint32_t f[32], xw[16];
+      tmem_ld32(tmem + lane_base + kColF + uint32_t(dg), f);
+      tmem_ld16(tmem + lane_base + kColX + uint32_t(dg / 2), xw);  // word i: dims dg + 2i, dg + 2i + 1
       tmem_wait_ld();
-      const unsigned char *xrow = sm + L::offX + (dg >> 6) * (kTileRows * 128) + (t >> 3) * 1024 + (t & 7) * 128;
 #pragma unroll
       for (int d = 0; d < 32; d += 4) {
-        const int chunk = ((dg & 63) + d) >> 3;  // 16-byte chunk within the 128-byte row
-        const uint2 xu = *reinterpret_cast<const uint2 *>(xrow + ((chunk ^ (t & 7)) << 4) + (d & 4) * 2);
-        const float2 x0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xu.x));
-        const float2 x1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xu.y));
+        const float2 x0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xw[d / 2]));
+        const float2 x1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xw[d / 2 + 1]));
         *reinterpret_cast<float4 *>(dst_row + dg + d) =
             make_float4(rowsum * x0.x - __uint_as_float(f[d]), rowsum * x0.y - __uint_as_float(f[d + 1]),
                         rowsum * x1.x - __uint_as_float(f[d + 2]), rowsum * x1.y - __uint_as_float(f[d + 3]));
@@ -695,18 +770,18 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       epi_sync();
       asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
       if (tid == 0) {
-        // this CTA's X tile is free and its INCOMING barrier expects the rows:
+        // this CTA's incoming area is free and its INCOMING barrier expects the rows:
         // tell the peer (a release arrive on the peer's PEER_FREE barrier)
         mbar_expect_tx(B(INCOMING), kInBytes);
         mbar_arrive_remote(peer_addr(B(PEER_FREE), peer));
       }
       // warp 0 pushes the partials of the peer's 64 rows, their flags and
-      // losses into the peer's X tile once the peer's X tile is free,
-      // completing on the peer's INCOMING barrier
+      // losses into the peer's shared memory once the peer has staged its own
+      // rows, completing on the peer's INCOMING barrier
       if (warp == 0 && __all_sync(kFull, mbar_wait_cluster(B(PEER_FREE), 0, &err))) {
         const int pr0 = peer * 64;
         const uint32_t pbar = peer_addr(B(INCOMING), peer);
-        const uint32_t in_base = peer_addr(smem_u32(sm + L::offX), peer);
+        const uint32_t in_base = peer_addr(smem_u32(in_rows), peer);
         for (int i = lane; i < 64; i += 32)
           bulk_s2peer(in_base + uint32_t(i * D * 4), smem_u32(stage + (pr0 + i) * kPitch), D * 4, pbar);
         if (lane == 0) {
@@ -738,7 +813,6 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       // the peer's copies into this CTA have landed, so the peer's staged rows
       // are no longer read: tell the peer at once
       if (tid == 0 && in_ok) mbar_arrive_remote(peer_addr(B(PEER_GOT), peer));
-      const float *in_rows = reinterpret_cast<const float *>(sm + L::offX);
       const int r0 = ks * 64;
       for (int i = warp; in_ok && i < 64; i += kEpiThreads / 32) {
         if (row_flags[r0 + i] == 0 || in_flags[i] == 0) continue;
