@@ -125,7 +125,6 @@ constexpr int kGatherTile = 32;
 template <int D>
 __global__ void __launch_bounds__(kGatherTile * 32) bf16_gather_kernel(const BF16BatchArgs a) {
   constexpr int N = D / 32;  // components per lane
-  pdl_trigger();  // the repulsion GEMMs may start their prologue (they wait before reading N)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int epoch = a.epoch[0];
   const int32_t *negs = a.negs + (size_t(epoch) * a.batches + a.batch_id) * a.ns;
@@ -424,12 +423,6 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   const int c_begin = ks == 0 ? 0 : (nchunks + 1) / 2;
   const int c_end = (KS == 1 || ks == 1) ? nchunks : (nchunks + 1) / 2;
   const int nloc = c_end - c_begin;
-  // Step lc of this CTA takes its chunk cl(lc) = (lc + rot) mod nloc: tiles
-  // start at different chunks, so at any moment the CTAs fetch different parts
-  // of N from L2 instead of all the same 32 KB (F and the loss sum the chunks in
-  // this order).
-  const int rot = (blockIdx.x / KS) % nloc;
-  auto cl = [&](int lc) { return lc + rot < nloc ? lc + rot : lc + rot - nloc; };
 
   // barrier ids
   constexpr int NST = L::kStages;
@@ -504,14 +497,11 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       mbar_expect_tx(B(FULL_X), L::kX);
       for (int ka = 0; ka < L::kAtoms; ++ka)
         tma_load_2d(sX + ka * kTileRows * 128, &map_x, ka * 64, a.base + tile_base, B(FULL_X));
-      // N comes from bf16_gather_kernel (launched just before, possibly still
-      // running under a programmatic dependency): wait for it
-      pdl_wait();
       // chunk lc into stage lc % NST once the second GEMM of chunk lc - NST has
       // read that stage; the last two stages are first free once the epilogue
       // warps have copied the X tile into tensor memory
       for (int lc = 0; lc < nloc && !failed(); ++lc) {
-        const int c = c_begin + cl(lc), st = lc % NST, use = lc / NST;
+        const int c = c_begin + lc, st = lc % NST, use = lc / NST;
         if (use > 0) {
           if (!mbar_wait_sleep(B(FREE_N + st), (use - 1) & 1, &err)) break;
         } else if (st >= NST - 2) {
@@ -630,9 +620,8 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
     const int32_t *nid_loc = a.nid + c_begin * kChunk;
     uint32_t *near_loc = a.near_bits + size_t(row_local) * kNearWords + c_begin * 2 + hf;
     const int et = hf * 128 + t;  // 0..255
-    pdl_wait();  // |n|^2 and ids come from bf16_gather_kernel
     if (et < kChunk)
-      negmeta[0][et] = make_float2(__ldg(nn_loc + cl(0) * kChunk + et), __int_as_float(__ldg(nid_loc + cl(0) * kChunk + et)));
+      negmeta[0][et] = make_float2(__ldg(nn_loc + et), __int_as_float(__ldg(nid_loc + et)));
     epi_sync();
     xx = xx_part[t] + xx_part[kTileRows + t];
 
@@ -645,8 +634,8 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       float pre_nn = 0.f;
       int pre_id = -1;
       if (pre) {
-        pre_nn = __ldg(nn_loc + cl(lc + 1) * kChunk + et);
-        pre_id = __ldg(nid_loc + cl(lc + 1) * kChunk + et);
+        pre_nn = __ldg(nn_loc + (lc + 1) * kChunk + et);
+        pre_id = __ldg(nid_loc + (lc + 1) * kChunk + et);
       }
       uint32_t s_raw[32] = {};
       const bool got = __all_sync(kFull, mbar_wait_sleep(B(S_FULL + b), (lc >> 1) & 1, &err));
@@ -717,7 +706,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         }
         rowsum += rs2.x + rs2.y;
       }
-      if (near_word) near_loc[cl(lc) * 2] = near_word;
+      if (near_word) near_loc[lc * 2] = near_word;
       if (pre) negmeta[b ^ 1][et] = make_float2(pre_nn, __int_as_float(pre_id));
       // every thread has read this chunk's S (which C overwrites: the row's other
       // half reads columns this half writes) and metadata; the next chunk's
@@ -1037,95 +1026,54 @@ namespace {
 
 // The repulsion GEMMs of a minibatch: one CTA per 128-row tile, or, with at
 // least two chunks of negatives, a cluster of two CTAs per tile that split them.
-// pdl: a programmatic dependency on the gather launched just before on s (the
-// prologue overlaps it); prio: the launch's scheduling priority (0: none).
 template <int D>
 cudaError_t launch_repulse(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn, int tiles,
-                           cudaStream_t s, bool pdl, int prio) {
-  const bool split = a.kpad / kChunk >= 2;
+                           cudaStream_t s) {
+  if (a.kpad / kChunk < 2) {
+    bf16_repulse_kernel<D, 1><<<tiles, kRepulseThreads, RepulseSmem<D>::dynamic, s>>>(mx, mn, a);
+    return cudaGetLastError();
+  }
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(split ? 2 * tiles : tiles);
+  cfg.gridDim = dim3(2 * tiles);
   cfg.blockDim = dim3(kRepulseThreads);
   cfg.dynamicSmemBytes = RepulseSmem<D>::dynamic;
   cfg.stream = s;
-  cudaLaunchAttribute attr[3];
-  int na = 0;
-  if (split) {
-    attr[na].id = cudaLaunchAttributeClusterDimension;
-    attr[na].val.clusterDim.x = 2;
-    attr[na].val.clusterDim.y = 1;
-    attr[na].val.clusterDim.z = 1;
-    ++na;
-  }
-  if (pdl) {
-    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[na].val.programmaticStreamSerializationAllowed = 1;
-    ++na;
-  }
-  if (prio) {
-    attr[na].id = cudaLaunchAttributePriority;
-    attr[na].val.priority = prio;
-    ++na;
-  }
-  cfg.attrs = attr;
-  cfg.numAttrs = na;
-  return split ? cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 2>, mx, mn, a)
-               : cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 1>, mx, mn, a);
-}
-
-// The gather of the negatives (at priority prio, 0: none).
-template <int D>
-cudaError_t launch_gather(const BF16BatchArgs &a, cudaStream_t s, int prio) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(a.kpad / kGatherTile);  // kpad: a multiple of 64
-  cfg.blockDim = dim3(kGatherTile * 32);
-  cfg.stream = s;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributePriority;
-  attr[0].val.priority = prio;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = prio ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, bf16_gather_kernel<D>, a);
-}
-
-// The highest scheduling priority of the device (numerically the least).
-int top_priority() {
-  static const int prio = [] {
-    int least = 0, greatest = 0;
-    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
-    return greatest;
-  }();
-  return prio;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, bf16_repulse_kernel<D, 2>, mx, mn, a);
 }
 
 template <int D, int U>
 cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
                                 cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                                cudaEvent_t fork, cudaEvent_t join, bool pdl) {
+                                cudaEvent_t fork, cudaEvent_t join) {
   const int item_ctas = (a.n_items + kPlainWarps - 1) / kPlainWarps;
+  const int gather_ctas = a.kpad / kGatherTile;  // kpad: a multiple of 64
   const int tiles = (a.rows + kTileRows - 1) / kTileRows;
   const int apply_ctas = (a.rows + 7) / 8;
   cudaError_t e = cudaSuccess;
   if (ev || !s2) {  // one after another (per-kernel timing)
     if (ev) cudaEventRecord(ev[0], s);
-    if ((e = launch_gather<D>(a, s, 0)) != cudaSuccess) return e;
+    bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
-    if ((e = launch_repulse<D>(a, mx, mn, tiles, s, false, 0)) != cudaSuccess) return e;
+    if ((e = launch_repulse<D>(a, mx, mn, tiles, s)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[3], s);
     bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
     return cudaGetLastError();
   }
   // the attractive pass and the negatives' path (gather, repulsion GEMMs) are
   // independent within a minibatch: they run on two streams, forked after the
-  // previous minibatch's update and joined before this one's.  The negatives'
-  // path is launched first and at the top priority, so the GEMM CTAs (one SM
-  // each) are placed before the attractive pass fills the SMs; the GEMMs'
-  // prologue overlaps the gather (programmatic dependency)
+  // previous minibatch's update and joined before this one's
   if ((e = cudaEventRecord(fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(s2, fork, 0)) != cudaSuccess) return e;
-  if ((e = launch_gather<D>(a, s2, top_priority())) != cudaSuccess) return e;
-  if ((e = launch_repulse<D>(a, mx, mn, tiles, s2, pdl, top_priority())) != cudaSuccess) return e;
+  bf16_gather_kernel<D><<<gather_ctas, kGatherTile * 32, 0, s2>>>(a);
+  if ((e = launch_repulse<D>(a, mx, mn, tiles, s2)) != cudaSuccess) return e;
   bf16_attract_kernel<D, U><<<item_ctas, kPlainWarps * 32, 0, s>>>(a);
   if ((e = cudaEventRecord(join, s2)) != cudaSuccess || (e = cudaStreamWaitEvent(s, join, 0)) != cudaSuccess) return e;
   bf16_apply_kernel<D><<<apply_ctas, 256, 0, s>>>(a);
@@ -1136,11 +1084,11 @@ cudaError_t launch_bf16_batch_d(const BF16BatchArgs &a, const CUtensorMap &mx, c
 
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
                               cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                              cudaEvent_t fork, cudaEvent_t join, bool pdl) {
+                              cudaEvent_t fork, cudaEvent_t join) {
   switch (dim) {
-    case 64: return launch_bf16_batch_d<64, 8>(a, mx, mn, s, ev, s2, fork, join, pdl);
-    case 128: return launch_bf16_batch_d<128, 8>(a, mx, mn, s, ev, s2, fork, join, pdl);
-    case 256: return launch_bf16_batch_d<256, 4>(a, mx, mn, s, ev, s2, fork, join, pdl);
+    case 64: return launch_bf16_batch_d<64, 8>(a, mx, mn, s, ev, s2, fork, join);
+    case 128: return launch_bf16_batch_d<128, 8>(a, mx, mn, s, ev, s2, fork, join);
+    case 256: return launch_bf16_batch_d<256, 4>(a, mx, mn, s, ev, s2, fork, join);
   }
   return cudaErrorInvalidValue;
 }

@@ -163,11 +163,10 @@ cudaError_t bf16_prepare(int dim);
 // repulsion GEMMs (on s2, forked and joined with the two events), then the
 // update with the exact close pairs.  ev (nullable): four events recorded before
 // the gather, attractive, GEMM and update launches, all on s one after another
-// (so is everything when s2 is null).  pdl: on s2 the GEMMs depend on the
-// gather programmatically (their prologue overlaps it).
+// (so is everything when s2 is null).
 cudaError_t launch_bf16_batch(int dim, const BF16BatchArgs &a, const CUtensorMap &mx, const CUtensorMap &mn,
                               cudaStream_t s, cudaEvent_t *ev, cudaStream_t s2,
-                              cudaEvent_t fork, cudaEvent_t join, bool pdl);
+                              cudaEvent_t fork, cudaEvent_t join);
 cudaError_t launch_bf16_flush(const BF16FlushArgs &a, cudaStream_t s);
 cudaError_t launch_f32_to_bf16(const float *src, __nv_bfloat16 *dst, int64_t count, cudaStream_t s);
 

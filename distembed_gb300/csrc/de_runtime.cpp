@@ -353,7 +353,7 @@ cudaError_t enqueue_epoch_bf16(de_handle *h, int ns, cudaStream_t st, cudaEvent_
     a.loss_row = h->d_loss_row;
     a.err = h->d_err;
     err = launch_bf16_batch(h->dim, a, h->map_x, h->map_n, st, ev ? ev + 4 * j : nullptr, h->stream2,
-                            h->ev_fork, h->ev_join, h->opt.pdl != 0);
+                            h->ev_fork, h->ev_join);
   }
   if (err == cudaSuccess) {
     BF16FlushArgs f{};
