@@ -336,13 +336,15 @@ struct RepulseSmem {
 //
 // KS = 2: the negatives of a tile are split between the two CTAs of a cluster
 // (rank 0: the first ceil(chunks / 2) chunks, rank 1 the rest), so twice as
-// many SMs work on a minibatch.  Rank r owns tile rows [64 r, 64 r + 64).  After
-// a cluster barrier (both CTAs done with their operand buffers) each CTA stages
-// its partial force (its row sums) x - (its F) of the rows it owns locally and
-// pushes those of the peer's rows into the peer's shared memory (posted stores
-// through distributed shared memory); after a second cluster barrier each CTA
-// adds the two partials of its rows from its own shared memory and stores them.
-// Partial sums are combined as own + peer, the same value on either rank.
+// many SMs work on a minibatch.  Rank r owns tile rows [64 r, 64 r + 64).  Each
+// CTA stages its partial force (its row sums) x - (its F) of all 128 rows in its
+// shared memory; once the peer has signalled (a release arrive on this CTA's
+// PEER_FREE barrier) that its incoming area is free, one warp pushes the peer's
+// 64 rows, their flags and losses with bulk copies into the peer's shared memory,
+// completing on the peer's INCOMING barrier; each CTA then adds the two partials
+// of its rows and stores them, and waits (PEER_GOT) until the peer has received
+// its rows before its shared memory ends.  Partial sums are combined as own +
+// peer, the same value on either rank.  Every wait is bounded.
 constexpr int kEpiThreads = 256;
 constexpr int kRepulseThreads = kEpiThreads + 64;
 
