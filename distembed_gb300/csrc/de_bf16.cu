@@ -99,6 +99,57 @@ __device__ __forceinline__ void store_f32_contig(const Frag<D> &f, float *row, i
 
 // ------------------------------------------------------------ attractive + gather
 
+// A lane's D/32 BF16 components of a row as loaded (16, 8 or 4 bytes), unpacked
+// to FP32 only when used, so that rows in flight cost half the registers.
+template <int D>
+struct RawRow {
+  static constexpr int W = D / 64;  // 32-bit words per lane
+  uint32_t w[W];
+};
+
+template <int D>
+__device__ __forceinline__ void load_raw(RawRow<D> &r, const __nv_bfloat16 *row, int lane) {
+  constexpr int W = RawRow<D>::W;
+  const __nv_bfloat16 *p = row + lane * (D / 32);
+  if constexpr (W == 4) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+    r.w[0] = u.x, r.w[1] = u.y, r.w[2] = u.z, r.w[3] = u.w;
+  } else if constexpr (W == 2) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
+    r.w[0] = u.x, r.w[1] = u.y;
+  } else {
+    static_assert(W == 1, "dim 64, 128 or 256");
+    r.w[0] = __ldg(reinterpret_cast<const unsigned *>(p));
+  }
+}
+
+// The same values load_bf16_row produces.
+template <int D>
+__device__ __forceinline__ void unpack_row(Frag<D> &f, const RawRow<D> &r) {
+#pragma unroll
+  for (int i = 0; i < RawRow<D>::W; ++i) {
+    const float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&r.w[i]));
+    f.v[2 * i] = t.x;
+    f.v[2 * i + 1] = t.y;
+  }
+}
+
+// The rows of CSR entries k .. k+U-1 (lane j of `ids`: the column of entry j,
+// -1 for none) as raw BF16; bit u of the result: entry k+u is a row.
+template <int D, int U>
+__device__ __forceinline__ unsigned fetch_group(const BF16BatchArgs &a, RawRow<D> (&raw)[U], int ids, int k, int lane) {
+  unsigned mask = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int n = __shfl_sync(kFull, ids, k + u);
+    if (n >= 0) {
+      load_raw<D>(raw[u], a.xb + size_t(n) * D, lane);
+      mask |= 1u << u;
+    }
+  }
+  return mask;
+}
+
 template <int D, int U>
 __device__ __forceinline__ void bf16_force_group(const BF16BatchArgs &a, Frag<D> &acc, const Frag<D> &xi, int ids,
                                                  int k, float lr, float bound, bool want_loss, float &loss,
@@ -194,8 +245,29 @@ __global__ void __launch_bounds__(kPlainWarps * 32, 6) bf16_attract_kernel(const
   load_bf16_row(xi, a.xb + size_t(a.base + it.row) * D, lane);
   acc.zero();
   float loss = 0.f;  // this item's loss terms (FP32); the epoch sum is FP64
-  int k = 0;  // groups of U; a last group of at most U/2 entries runs as a group of U/2
-  for (; k + U / 2 < cnt; k += U) bf16_force_group<D, U>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
+  // groups of U, software-pipelined: the next group's rows are in flight (as
+  // raw BF16) while this group's forces are computed; a last group of at most
+  // U/2 entries runs as a group of U/2
+  int k = 0;
+  if (U / 2 < cnt) {
+    RawRow<D> cur[U];
+    unsigned mcur = fetch_group<D, U>(a, cur, ids, 0, lane);
+    for (; k + U / 2 < cnt; k += U) {
+      RawRow<D> nxt[U];
+      unsigned mnxt = 0;
+      if (k + U + U / 2 < cnt) mnxt = fetch_group<D, U>(a, nxt, ids, k + U, lane);
+      Frag<D> xn[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if ((mcur >> u) & 1u) unpack_row<D>(xn[u], cur[u]);
+        else xn[u] = xi;
+      }
+      if (mcur) pair_forces<D, U, true>(acc, xi, xn, mcur, lr, a.bound, want_loss, loss, lane);
+#pragma unroll
+      for (int u = 0; u < U; ++u) cur[u] = nxt[u];
+      mcur = mnxt;
+    }
+  }
   if (k < cnt) bf16_force_group<D, U / 2>(a, acc, xi, ids, k, lr, a.bound, want_loss, loss, lane);
 
   bool owner = true;
