@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -319,16 +320,23 @@ int prepare_batched(de_batch *b, int epochs, int B, int ns, const double *lr, co
     total += size_t(epochs) * b->ginfo[g].batches * ns;
   }
   std::vector<int32_t> negs(std::max<size_t>(total, 1));
-  std::vector<int64_t> draw(std::max(ns, 1));
-  for (int g = 0; g < b->n_graphs; ++g) {
-    const GraphInfo &G = b->ginfo[g];
-    for (int e = 0; e < epochs; ++e)
-      for (int j = 0; j < G.batches; ++j) {
-        de_negatives(G.n, e + j, ns, draw.data());
-        int32_t *o = negs.data() + G.neg_off + (size_t(e) * G.batches + j) * ns;
-        for (int q = 0; q < ns; ++q) o[q] = int32_t(draw[q]);
-      }
-  }
+  // minibatch q of the run (graphs in order, then epochs, then minibatches) owns
+  // negs[q * ns, (q + 1) * ns); its draws depend only on its graph and seed, so
+  // they are made on host threads
+  std::vector<int64_t> mb_end(b->n_graphs);  // minibatches up to and including graph g
+  int64_t mbs = 0;
+  for (int g = 0; g < b->n_graphs; ++g) mb_end[g] = (mbs += int64_t(epochs) * b->ginfo[g].batches);
+  if (ns > 0)
+    de::parallel_indices(mbs, ns, [&](int64_t q) {
+      const int g = int(std::upper_bound(mb_end.begin(), mb_end.end(), q) - mb_end.begin());
+      const GraphInfo &G = b->ginfo[g];
+      const int64_t local = q - (mb_end[g] - int64_t(epochs) * G.batches);
+      const int e = int(local / G.batches), j = int(local % G.batches);
+      std::minstd_rand gen(e + j);  // the sampler of de_negatives (seed = epoch + batch)
+      std::uniform_int_distribution<int> dist(0, int(G.n));
+      int32_t *o = negs.data() + size_t(q) * ns;
+      for (int k = 0; k < ns; ++k) o[k] = dist(gen);
+    });
   std::vector<float> lrf(epochs);
   for (int e = 0; e < epochs; ++e) lrf[e] = float(lr[e]);
   if (int rc = bgrow(b, &b->d_negs, &b->negs_cap, negs.size())) return rc;

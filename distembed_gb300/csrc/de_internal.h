@@ -7,10 +7,36 @@
 
 #include "../../include/distembed_gb300.h"
 
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace de {
+
+// f(i) for i in [0, count), on host threads when count * cost_per_item is large
+// (contiguous index ranges, one per thread; f must write only what index i owns,
+// so the result does not depend on the split).
+template <class F>
+void parallel_indices(int64_t count, int64_t cost_per_item, F &&f) {
+  int threads = 1;
+  if (count * cost_per_item >= (int64_t(1) << 18))
+    threads = int(std::min<int64_t>({int64_t(std::max(1u, std::thread::hardware_concurrency())), 32, count}));
+  if (threads <= 1) {
+    for (int64_t i = 0; i < count; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const int64_t per = (count + threads - 1) / threads;
+  for (int t = 0; t < threads; ++t) {
+    const int64_t lo = t * per, hi = std::min(count, lo + per);
+    if (lo >= hi) break;
+    pool.emplace_back([&f, lo, hi] {
+      for (int64_t i = lo; i < hi; ++i) f(i);
+    });
+  }
+  for (auto &th : pool) th.join();
+}
 
 // One unit of attractive work: row `row` (index within its minibatch) over CSR
 // entries [e_begin, e_end).  Rows whose degree exceeds the edge cap are split

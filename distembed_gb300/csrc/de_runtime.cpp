@@ -823,9 +823,13 @@ static int prepare_run(de_handle *h, int32_t first_epoch, int32_t epochs, int32_
       (rc = grow_pinned(h, &h->h_lr, &h->h_lr_cap, size_t(epochs))) ||
       (rc = grow_pinned(h, &h->h_loss, &h->h_loss_cap, size_t(epochs))))
     return rc;
-  for (int i = 0; i < epochs; ++i)
-    for (int j = 0; j < s.batches; ++j)
-      draw_negatives(h->n, first_epoch + i + j, ns, h->h_negs + (size_t(i) * s.batches + j) * ns);
+  // the draws of minibatch j of epoch i at (i * batches + j) * ns; many runs'
+  // worth (e.g. 10 epochs x 512 minibatches x 1024 draws) on host threads
+  const int64_t batches = s.batches;
+  parallel_indices(int64_t(epochs) * batches, std::max(ns, 1), [&](int64_t q) {
+    const int i = int(q / batches), j = int(q % batches);
+    draw_negatives(h->n, first_epoch + i + j, ns, h->h_negs + size_t(q) * ns);
+  });
   for (int i = 0; i < epochs; ++i) h->h_lr[i] = float(lr_per_epoch[i]);
   DE_CUDA(h, cudaMemcpyAsync(h->d_negs, h->h_negs, nneg * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   DE_CUDA(h, cudaMemcpyAsync(h->d_lr, h->h_lr, epochs * sizeof(float), cudaMemcpyHostToDevice, h->stream));
