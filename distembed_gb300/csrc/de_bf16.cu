@@ -554,15 +554,17 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
   int *const in_flags = reinterpret_cast<int *>(misc + 8192);
   double *const in_loss = reinterpret_cast<double *>(misc + 8448);
   // after the GEMMs: the staged force rows (pitch D + 4 floats) over the N
-  // stages; KS = 2: after them the peer's partials of this CTA's 64 rows (pitch
-  // D floats, reaching 2048 B into the then dead half-row exchange area), their
-  // 64 flags and 64 losses in the misc area
+  // stages; KS = 2: after them the peer's partials of this CTA's 64 rows (the
+  // same pitch: one contiguous block, reaching into the then dead half-row
+  // exchange area of misc, before the row flags), their 64 flags and 64 losses
+  // in the misc area
   constexpr int kPitch = D + 4;
   constexpr int kStageBytes = kTileRows * kPitch * 4;
+  constexpr uint32_t kHalfRowsBytes = 64 * kPitch * 4;
   float *const stage = reinterpret_cast<float *>(sm + L::offN);
   float *const in_rows = reinterpret_cast<float *>(sm + L::offN + kStageBytes);
-  static_assert(kStageBytes + 64 * D * 4 <= L::offMisc - L::offN + 2048, "incoming rows end before loss_part");
-  constexpr uint32_t kInBytes = 64 * D * 4 + 64 * 4 + 64 * 8;
+  static_assert(kStageBytes + kHalfRowsBytes <= L::offMisc - L::offN + 4096, "incoming rows end before the row flags");
+  constexpr uint32_t kInBytes = kHalfRowsBytes + 64 * 4 + 64 * 8;
 
   if (warp == 8) {
     // ---------------- TMA producer
@@ -838,16 +840,15 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
         mbar_expect_tx(B(INCOMING), kInBytes);
         mbar_arrive_remote(peer_addr(B(PEER_FREE), peer));
       }
-      // warp 0 pushes the partials of the peer's 64 rows, their flags and
-      // losses into the peer's shared memory once the peer has staged its own
-      // rows, completing on the peer's INCOMING barrier
+      // warp 0 pushes the partials of the peer's 64 rows (one contiguous block
+      // of staged rows), their flags and losses into the peer's shared memory
+      // once the peer has staged its own rows, completing on the peer's
+      // INCOMING barrier
       if (warp == 0 && __all_sync(kFull, mbar_wait_cluster(B(PEER_FREE), 0, &err))) {
         const int pr0 = peer * 64;
         const uint32_t pbar = peer_addr(B(INCOMING), peer);
-        const uint32_t in_base = peer_addr(smem_u32(in_rows), peer);
-        for (int i = lane; i < 64; i += 32)
-          bulk_s2peer(in_base + uint32_t(i * D * 4), smem_u32(stage + (pr0 + i) * kPitch), D * 4, pbar);
         if (lane == 0) {
+          bulk_s2peer(peer_addr(smem_u32(in_rows), peer), smem_u32(stage + pr0 * kPitch), kHalfRowsBytes, pbar);
           bulk_s2peer(peer_addr(smem_u32(in_flags), peer), smem_u32(&row_flags[pr0]), 64 * 4, pbar);
           bulk_s2peer(peer_addr(smem_u32(in_loss), peer), smem_u32(&row_loss[pr0]), 64 * 8, pbar);
         }
@@ -880,7 +881,7 @@ __global__ void __launch_bounds__(kRepulseThreads, 1) bf16_repulse_kernel(const 
       for (int i = warp; in_ok && i < 64; i += kEpiThreads / 32) {
         if (row_flags[r0 + i] == 0 || in_flags[i] == 0) continue;
         const float4 *own = reinterpret_cast<const float4 *>(stage + (r0 + i) * kPitch);
-        const float4 *oth = reinterpret_cast<const float4 *>(in_rows + i * D);
+        const float4 *oth = reinterpret_cast<const float4 *>(in_rows + i * kPitch);
         float4 *rbp = reinterpret_cast<float4 *>(a.rbuf + size_t(tile_base + r0 + i) * D);
 #pragma unroll
         for (int v = lane; v < D / 4; v += 32) {
